@@ -1,0 +1,202 @@
+/*
+ * ohpic.h -- C ABI of the GB300 particle hot path for ohhelppic3d.
+ *
+ * The reference (Nkzono99/ohhelppic3d, Fortran 2008) advances particles one
+ * record at a time through polymorphic type-bound procedures:
+ *
+ *   t_Scatter%scatter(particle, ohfield, amount, ps)       src/scatter/scatter.f90:15-24
+ *   t_FieldSolver%solve(rho, aj, eb, phi, ohhelp)          src/field_solver/field_solver.f90:15-25
+ *   t_Interpolator%interp(particle, field, ps) -> ret(6)   src/interpolator/interpolator.f90:16-25
+ *   t_ParticleMover%move(particle, qm, eb, dt)             src/particle_mover/particle_mover.f90:16-24
+ *   t_ParticleBoundary%apply(particle, dt)                 src/particle_boundary/particle_boundary.f90:14-20
+ *
+ * called from the loops of mainstep (src/ohhelppic3d.f90:311-358).  A call per
+ * particle across a language boundary cannot feed a GPU, so this ABI offers the
+ * same operations batched over every particle of the run, with the particles
+ * and fields resident in device memory between calls.  The Fortran side binds
+ * these functions with ISO_C_BINDING (the interface block is given in
+ * INTEGRATION.md).
+ *
+ * Conventions
+ *   - Every function returns an int status: OHPIC_OK (0) or an OHPIC_ERR_* code.
+ *     No C++ exception crosses the ABI.  ohpic_last_error() gives the message.
+ *   - Host arrays are borrowed for the duration of the call only.
+ *   - Work is ordered on the context's own CUDA stream.  Calls that return host
+ *     data (download, diagnostics) synchronise that stream; the others do not.
+ *   - One context belongs to one host thread at a time.
+ *   - Fields are exchanged as nx*ny*nz doubles with x fastest, which is the
+ *     interior of the reference's t_OhField%values(1, 0:nx-1, 0:ny-1, 0:nz-1, 1)
+ *     (src/ohhelp/ohfield.f90:54,165-169); ohpic_download_field_ohfield() fills
+ *     the full layout including halos.
+ */
+#ifndef OHPIC_H
+#define OHPIC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OHPIC_MAX_SPECIES 8
+#define OHPIC_ABI_VERSION 1
+
+/* Status codes. */
+enum {
+    OHPIC_OK = 0,
+    OHPIC_ERR_INVALID = 1,      /* bad argument or configuration */
+    OHPIC_ERR_OOM = 2,          /* device or pinned-host allocation failed */
+    OHPIC_ERR_CUDA = 3,         /* a CUDA / cuFFT call failed */
+    OHPIC_ERR_BOUNDS = 4,       /* a kernel saw an index outside its grid (device error flag) */
+    OHPIC_ERR_TIMEOUT = 5,      /* a bounded device wait ran out */
+    OHPIC_ERR_CAPACITY = 6,     /* more particles than the species capacity */
+    OHPIC_ERR_UNSUPPORTED = 7,  /* the reference's per-particle entry points (see below) */
+    OHPIC_ERR_NONFINITE = 8,    /* NaN or Inf in the particle state */
+    OHPIC_ERR_REJECTED = 9      /* serving: request does not fit the memory budget */
+};
+
+/* Precision forms. */
+enum {
+    OHPIC_FP64 = 0,  /* plain form: absolute FP64 positions and velocities */
+    OHPIC_FP32 = 1   /* precision form: int32 cell + FP32 in-cell offset, FP32 velocity */
+};
+
+/* CIC weight convention.  The reference gives node floor(x) the weight
+ * r = x - floor(x) and node floor(x)+1 the weight 1-r
+ * (src/interpolator/linear_interpolator.f90:54-64, src/scatter/linear_scatter.f90:41-52);
+ * OHPIC_WEIGHTS_STANDARD is the textbook assignment (1-r, r). */
+enum { OHPIC_WEIGHTS_REFERENCE = 0, OHPIC_WEIGHTS_STANDARD = 1 };
+
+/* Field selectors. */
+enum { OHPIC_RHO = 0, OHPIC_PHI = 1, OHPIC_EX = 2, OHPIC_EY = 3, OHPIC_EZ = 4 };
+
+typedef struct ohpic_config {
+    int32_t nx, ny, nz;         /* periodic grid, dx = 1 (parameters.f90:209-211) */
+    int32_t nspecies;           /* 1..OHPIC_MAX_SPECIES (parameters.f90:239) */
+    int32_t precision;          /* OHPIC_FP64 or OHPIC_FP32 */
+    int32_t weights;            /* OHPIC_WEIGHTS_* */
+    int32_t sort_every;         /* cell sort cadence in steps; 0 = only explicit ohpic_sort */
+    int32_t tile[3];            /* tile shape in cells; 0 = tuned default */
+    int32_t track_ids;          /* 1: keep a per-particle id through sorts */
+    int32_t device;             /* CUDA device ordinal */
+    double dt;                  /* default time step (parameters.f90:213) */
+    double b0[3];               /* uniform magnetic field passed to Boris */
+    double qm[OHPIC_MAX_SPECIES];   /* charge-to-mass ratio (parameters.f90:240) */
+    double q[OHPIC_MAX_SPECIES];    /* charge per macro-particle (parameters.f90:259-260) */
+    int64_t capacity[OHPIC_MAX_SPECIES]; /* maximum particles per species */
+} ohpic_config;
+
+typedef struct ohpic_diag {
+    int64_t count[OHPIC_MAX_SPECIES];
+    int64_t crossings[3];       /* particles that wrapped along x, y, z in the last push */
+    int64_t outside_tile;       /* particles the last push served from global memory */
+    int64_t step;               /* pushes since creation */
+    double total_charge;        /* sum of rho over nodes (FP64 reduction) */
+    double field_energy;        /* 0.5 * sum |E|^2 over nodes */
+    double kinetic_energy;      /* sum 0.5 * (q/qm) |v|^2 over particles */
+    double momentum[3];         /* sum (q/qm) v */
+} ohpic_diag;
+
+typedef struct ohpic_ctx ohpic_ctx;
+
+/* Fills cfg with defaults (FP64 form, reference weights, sort every 20 steps,
+ * tuned tiles, ids tracked, device 0).  Grid, species and dt stay zero. */
+void ohpic_config_default(ohpic_config *cfg);
+
+/* Creates a context that owns all device memory and one CUDA stream.
+ * Replaces the set-up of src/ohhelppic3d.f90:114-122 (field allocation),
+ * :195 (new_LinearScatter), :261-269 (new_PoissonFieldSolver), :273
+ * (new_LinearInterpolator) and :279-282 (mover factory and boundaries). */
+int ohpic_create(const ohpic_config *cfg, ohpic_ctx **out);
+int ohpic_destroy(ohpic_ctx *ctx);
+
+/* Particle transfer.  The AoS form reads records of stride_bytes whose first
+ * six doubles are x, y, z, vx, vy, vz, i.e. the leading members of the
+ * reference's oh_particle (src/ohhelp/ohparticles.f90:17, used by
+ * particle_injector_with_distribution.f90:196-201).  Upload replaces the
+ * species' particles; n may be 0. */
+int ohpic_upload_particles(ohpic_ctx *ctx, int species, const void *pbuf, int64_t n,
+                           int64_t stride_bytes);
+int ohpic_upload_particles_soa(ohpic_ctx *ctx, int species, const double *x, const double *y,
+                               const double *z, const double *vx, const double *vy,
+                               const double *vz, int64_t n);
+/* Download in device order; ids (nullable) receive each particle's index in
+ * the last upload, so a caller can restore its own order. */
+int ohpic_download_particles_soa(ohpic_ctx *ctx, int species, double *x, double *y, double *z,
+                                 double *vx, double *vy, double *vz, uint32_t *ids,
+                                 int64_t capacity, int64_t *n_out);
+int ohpic_download_particles(ohpic_ctx *ctx, int species, void *pbuf, int64_t capacity,
+                             int64_t stride_bytes, int64_t *n_out);
+
+/* t_Scatter%scatter over every particle (linear_scatter.f90:22-55 driven by
+ * ohhelppic3d.f90:311-320): rho = 0, CIC deposit of q_s, periodic fold. */
+int ohpic_scatter(ohpic_ctx *ctx);
+
+/* t_FieldSolver%solve (poisson_field_solver.f90:90-175): spectral Poisson
+ * solve of rho (poisson_solver3d.f90:134-207) and E = -grad phi by the
+ * staggered difference plus two-point average. */
+int ohpic_solve(ohpic_ctx *ctx);
+
+/* t_Interpolator%interp over every particle of one species: e_out receives
+ * 3*n doubles (Ex, Ey, Ez per particle) in device order. */
+int ohpic_interp(ohpic_ctx *ctx, int species, double *e_out, int64_t capacity, int64_t *n_out);
+
+/* t_ParticleMover%move (Boris, particle_mover_boris.f90:21-64) followed by
+ * t_ParticleBoundaries%apply twice (ohhelppic3d.f90:353,355) over every
+ * particle, gathering E from the last solve.  Leaves rho stale. */
+int ohpic_move(ohpic_ctx *ctx, double dt);
+
+/* Fused gather + Boris + periodic wrap + deposit of the new positions: one
+ * read and one write of each particle, after which rho holds the charge
+ * the next mainstep would scatter. */
+int ohpic_push(ohpic_ctx *ctx, double dt);
+
+/* nsteps x mainstep: solve, push, and the cell sort every sort_every steps.
+ * Scatters first if rho is stale. */
+int ohpic_step(ohpic_ctx *ctx, double dt, int nsteps);
+
+/* Periodic counting sort of every species by tile-major cell index. */
+int ohpic_sort(ohpic_ctx *ctx);
+
+/* Field exchange, nx*ny*nz doubles with x fastest.  Uploading rho or E
+ * replaces the device copy (for isolated tests of solve or move). */
+int ohpic_download_field(ohpic_ctx *ctx, int which, double *host);
+int ohpic_upload_field(ohpic_ctx *ctx, int which, const double *host);
+
+/* Download into the reference's t_OhField%values(nelem, lo:hi, ...) layout for
+ * one field slot (ohfield.f90:165-169): values has nelem leading elements per
+ * node (1 for rho/phi, 6 for eb, whose elements 1-3 receive E and 4-6 B0) and
+ * node ranges lo[d]..hi[d] (inclusive, may extend past the grid as halos,
+ * filled periodically).  which: OHPIC_RHO, OHPIC_PHI or OHPIC_EX (whole eb). */
+int ohpic_download_field_ohfield(ohpic_ctx *ctx, int which, double *values, int nelem,
+                                 const int32_t lo[3], const int32_t hi[3]);
+
+int ohpic_diagnostics(ohpic_ctx *ctx, ohpic_diag *out);
+
+/* The per-particle bindings of the reference cannot be served from device
+ * memory; the batched calls above replace them.  These return
+ * OHPIC_ERR_UNSUPPORTED so a caller that still loops per particle fails loudly. */
+int ohpic_move_one(ohpic_ctx *ctx, double *particle, double qm, const double *eb, double dt);
+int ohpic_scatter_one(ohpic_ctx *ctx, const double *particle, double amount, int ps);
+
+/* Copies the last error message (NUL-terminated, truncated to len). */
+int ohpic_last_error(const ohpic_ctx *ctx, char *buf, size_t len);
+/* Message of a status code. */
+const char *ohpic_status_string(int status);
+
+int ohpic_synchronize(ohpic_ctx *ctx);
+/* The context's cudaStream_t, for callers that order their own work after it. */
+int ohpic_get_stream(ohpic_ctx *ctx, void **stream);
+
+/* Instrumentation: kernel launches issued by this context so far, and the
+ * summed CUDA-event duration of the fused push kernel (enable first). */
+int ohpic_set_push_timing(ohpic_ctx *ctx, int enable);
+int ohpic_stats(ohpic_ctx *ctx, int64_t *launches, int64_t *push_launches, double *push_ms);
+/* Device bytes held by the context. */
+int ohpic_memory(ohpic_ctx *ctx, int64_t *device_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,304 @@
+// fields.cu -- spectral Poisson solve and the E stencil.
+//
+// Reference: t_PoissonFieldSolver%solve (src/field_solver/poisson_field_solver.f90:90-175)
+//   phi = rho; forward R2HC x3; divide by the modified wave number
+//   sum_d (2 sin(pi k_d / n_d))^2 (poisson_solver3d.f90:104-117, :184-192); zero k = 0
+//   (:194-198); backward HC2R x3 and divide by nx*ny*nz (mpi_fftw3_solver.f90:223-236);
+//   then E_d[i] = phi[i] - phi[i+e_d] (:131-145) and E_d[i] = (E_d[i-e_d] + E_d[i]) / 2
+//   (:157-171), which combine to E_d[i] = 0.5*((phi[i-e] - phi[i]) + (phi[i] - phi[i+e])).
+//
+// The tensor-product real half-complex basis of the reference and the R2C
+// transform used here diagonalise the same periodic 7-point Laplacian, with the
+// same eigenvalue per wave vector, so dividing the cuFFT half spectrum by that
+// eigenvalue gives the reference's phi up to rounding.  The Green table holds
+// 1/(eigenvalue * nx*ny*nz) in FP64 (0 at k = 0) and is built once on the device
+// with the reference's truncated pi literal (src/utils/science_constants.f90:4).
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stdint.h>
+
+#include "ohpic_internal.cuh"
+
+namespace ohpic {
+namespace {
+
+constexpr double kRefPi = 3.14159265358979;
+
+__device__ __forceinline__ double wave_number(int k, int n)
+{
+    // poisson_solver3d.f90:114-117
+    if (k <= n / 2) return 2.0 * sin(kRefPi * k / (double)n);
+    return 2.0 * sin(kRefPi * (n - k) / (double)n);
+}
+
+__global__ void k_green(Geom g, double *green)
+{
+    const int64_t total = g.nspec;
+    const double norm = (double)g.nx * (double)g.ny * (double)g.nz;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int kx = (int)(i % g.nxh);
+        const int ky = (int)((i / g.nxh) % g.ny);
+        const int kz = (int)(i / ((int64_t)g.nxh * g.ny));
+        if (kx == 0 && ky == 0 && kz == 0) {
+            green[i] = 0.0;
+            continue;
+        }
+        const double wx = wave_number(kx, g.nx), wy = wave_number(ky, g.ny), wz = wave_number(kz, g.nz);
+        const double wn = wx * wx + wy * wy + wz * wz;
+        green[i] = 1.0 / (wn * norm);
+    }
+}
+
+__global__ void k_scale_z(cufftDoubleComplex *spec, const double *green, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double gf = green[i];
+        cufftDoubleComplex v = spec[i];
+        v.x *= gf;
+        v.y *= gf;
+        spec[i] = v;
+    }
+}
+
+// FP32 spectrum scaled by the FP64 table in FP64 arithmetic.
+__global__ void k_scale_c(cufftComplex *spec, const double *green, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double gf = green[i];
+        cufftComplex v = spec[i];
+        v.x = (float)((double)v.x * gf);
+        v.y = (float)((double)v.y * gf);
+        spec[i] = v;
+    }
+}
+
+__device__ __forceinline__ int wrapn(int i, int n)
+{
+    i %= n;
+    return i < 0 ? i + n : i;
+}
+
+// phi (n^3) -> padded E nodes, periodic ghosts included.
+template <typename T, typename NodeT>
+__global__ void k_stencil(Geom g, const T *phi, NodeT *epad)
+{
+    const int64_t total = (int64_t)g.gx * g.gy * g.gz;
+    const int64_t nxy = (int64_t)g.nx * g.ny;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int px = (int)(t % g.gx);
+        const int py = (int)((t / g.gx) % g.gy);
+        const int pz = (int)(t / ((int64_t)g.gx * g.gy));
+        const int i = wrapn(px - g.halo, g.nx), j = wrapn(py - g.halo, g.ny), k = wrapn(pz - g.halo, g.nz);
+        const int im = i == 0 ? g.nx - 1 : i - 1, ip = i + 1 == g.nx ? 0 : i + 1;
+        const int jm = j == 0 ? g.ny - 1 : j - 1, jp = j + 1 == g.ny ? 0 : j + 1;
+        const int km = k == 0 ? g.nz - 1 : k - 1, kp = k + 1 == g.nz ? 0 : k + 1;
+        const int64_t row = (int64_t)j * g.nx + (int64_t)k * nxy;
+        const T p0 = phi[i + row];
+        NodeT e;
+        e.x = T(0.5) * ((phi[im + row] - p0) + (p0 - phi[ip + row]));
+        e.y = T(0.5) * ((phi[i + (int64_t)jm * g.nx + (int64_t)k * nxy] - p0) +
+                        (p0 - phi[i + (int64_t)jp * g.nx + (int64_t)k * nxy]));
+        e.z = T(0.5) * ((phi[i + row - (int64_t)k * nxy + (int64_t)km * nxy] - p0) +
+                        (p0 - phi[i + row - (int64_t)k * nxy + (int64_t)kp * nxy]));
+        e.w = T(0);
+        epad[t] = e;
+    }
+}
+
+// One n^3 FP64 component array -> that component of every padded E node (uploaded E).
+template <typename T, typename NodeT>
+__global__ void k_fill_epad(Geom g, const double *src, int comp, NodeT *epad)
+{
+    const int64_t total = (int64_t)g.gx * g.gy * g.gz;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int px = (int)(t % g.gx);
+        const int py = (int)((t / g.gx) % g.gy);
+        const int pz = (int)(t / ((int64_t)g.gx * g.gy));
+        const int i = wrapn(px - g.halo, g.nx), j = wrapn(py - g.halo, g.ny), k = wrapn(pz - g.halo, g.nz);
+        const T v = (T)src[i + (int64_t)g.nx * (j + (int64_t)g.ny * k)];
+        if (comp == 0) epad[t].x = v;
+        else if (comp == 1) epad[t].y = v;
+        else epad[t].z = v;
+    }
+}
+
+// Interior of the padded E -> one FP64 component array.
+template <typename NodeT>
+__global__ void k_epad_component(Geom g, const NodeT *epad, int comp, double *out)
+{
+    const int64_t total = g.ncell;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(t % g.nx);
+        const int j = (int)((t / g.nx) % g.ny);
+        const int k = (int)(t / ((int64_t)g.nx * g.ny));
+        const NodeT e = epad[(i + g.halo) + (int64_t)g.gx * ((j + g.halo) + (int64_t)g.gy * (k + g.halo))];
+        out[t] = comp == 0 ? (double)e.x : comp == 1 ? (double)e.y : (double)e.z;
+    }
+}
+
+template <typename T>
+__global__ void k_to_double(const T *in, double *out, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+
+template <typename T>
+__global__ void k_from_double(const double *in, T *out, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (T)in[i];
+}
+
+// FP64 reductions: sum of rho and 0.5 * sum |E|^2 over interior nodes.
+template <typename T, typename NodeT>
+__global__ void k_field_sums(Geom g, const T *rho, const NodeT *epad, double *charge, double *energy)
+{
+    double q = 0.0, e2 = 0.0;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < g.ncell; t += (int64_t)gridDim.x * blockDim.x) {
+        q += (double)rho[t];
+        const int i = (int)(t % g.nx);
+        const int j = (int)((t / g.nx) % g.ny);
+        const int k = (int)(t / ((int64_t)g.nx * g.ny));
+        const NodeT e = epad[(i + g.halo) + (int64_t)g.gx * ((j + g.halo) + (int64_t)g.gy * (k + g.halo))];
+        e2 += (double)e.x * (double)e.x + (double)e.y * (double)e.y + (double)e.z * (double)e.z;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        q += __shfl_xor_sync(0xffffffffu, q, o);
+        e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(charge, q);
+        atomicAdd(energy, 0.5 * e2);
+    }
+}
+
+int blocks_for(int64_t n)
+{
+    int64_t b = (n + 255) / 256;
+    if (b > 152 * 16) b = 152 * 16;
+    return b < 1 ? 1 : (int)b;
+}
+
+}  // namespace
+
+int fields_setup(ohpic_ctx *c)
+{
+    const Geom &g = c->g;
+    cufftResult r;
+    if (c->cfg.precision == OHPIC_FP64) {
+        r = cufftPlan3d(&c->plan_r2c, g.nz, g.ny, g.nx, CUFFT_D2Z);
+        if (r == CUFFT_SUCCESS) r = cufftPlan3d(&c->plan_c2r, g.nz, g.ny, g.nx, CUFFT_Z2D);
+    } else {
+        r = cufftPlan3d(&c->plan_r2c, g.nz, g.ny, g.nx, CUFFT_R2C);
+        if (r == CUFFT_SUCCESS) r = cufftPlan3d(&c->plan_c2r, g.nz, g.ny, g.nx, CUFFT_C2R);
+    }
+    if (r != CUFFT_SUCCESS) {
+        c->err = "cufftPlan3d failed (" + std::to_string((int)r) + ")";
+        return OHPIC_ERR_CUDA;
+    }
+    c->plans_made = true;
+    cufftSetStream(c->plan_r2c, c->stream);
+    cufftSetStream(c->plan_c2r, c->stream);
+    k_green<<<blocks_for(g.nspec), 256, 0, c->stream>>>(g, c->green);
+    ++c->launches;
+    return OHPIC_OK;
+}
+
+void fields_teardown(ohpic_ctx *c)
+{
+    if (c->plans_made) {
+        cufftDestroy(c->plan_r2c);
+        cufftDestroy(c->plan_c2r);
+        c->plans_made = false;
+    }
+}
+
+int solve_fields(ohpic_ctx *c)
+{
+    const Geom &g = c->g;
+    cufftResult r;
+    if (c->cfg.precision == OHPIC_FP64) {
+        r = cufftExecD2Z(c->plan_r2c, (cufftDoubleReal *)c->rho, (cufftDoubleComplex *)c->spec);
+        if (r != CUFFT_SUCCESS) goto fail;
+        k_scale_z<<<blocks_for(g.nspec), 256, 0, c->stream>>>((cufftDoubleComplex *)c->spec, c->green, g.nspec);
+        r = cufftExecZ2D(c->plan_c2r, (cufftDoubleComplex *)c->spec, (cufftDoubleReal *)c->phi);
+        if (r != CUFFT_SUCCESS) goto fail;
+        k_stencil<double, dnode><<<blocks_for((int64_t)g.gx * g.gy * g.gz), 256, 0, c->stream>>>(
+            g, (const double *)c->phi, (dnode *)c->epad);
+    } else {
+        r = cufftExecR2C(c->plan_r2c, (cufftReal *)c->rho, (cufftComplex *)c->spec);
+        if (r != CUFFT_SUCCESS) goto fail;
+        k_scale_c<<<blocks_for(g.nspec), 256, 0, c->stream>>>((cufftComplex *)c->spec, c->green, g.nspec);
+        r = cufftExecC2R(c->plan_c2r, (cufftComplex *)c->spec, (cufftReal *)c->phi);
+        if (r != CUFFT_SUCCESS) goto fail;
+        k_stencil<float, float4><<<blocks_for((int64_t)g.gx * g.gy * g.gz), 256, 0, c->stream>>>(
+            g, (const float *)c->phi, (float4 *)c->epad);
+    }
+    c->launches += 2;
+    return OHPIC_OK;
+fail:
+    c->err = "cuFFT exec failed (" + std::to_string((int)r) + ")";
+    return OHPIC_ERR_CUDA;
+}
+
+void launch_zero(ohpic_ctx *c, void *p, int64_t bytes) { cudaMemsetAsync(p, 0, (size_t)bytes, c->stream); }
+
+void launch_field_energy(ohpic_ctx *c)
+{
+    const Geom &g = c->g;
+    cudaMemsetAsync(&c->diag->charge, 0, 2 * sizeof(double), c->stream);
+    if (c->cfg.precision == OHPIC_FP64)
+        k_field_sums<double, dnode><<<blocks_for(g.ncell), 256, 0, c->stream>>>(
+            g, (const double *)c->rho, (const dnode *)c->epad, &c->diag->charge, &c->diag->field_energy);
+    else
+        k_field_sums<float, float4><<<blocks_for(g.ncell), 256, 0, c->stream>>>(
+            g, (const float *)c->rho, (const float4 *)c->epad, &c->diag->charge, &c->diag->field_energy);
+    ++c->launches;
+}
+
+// Field transfers through a device staging buffer of >= 3*ncell doubles.
+void field_to_double(ohpic_ctx *c, int which, double *dst)
+{
+    const Geom &g = c->g;
+    const bool f64 = c->cfg.precision == OHPIC_FP64;
+    if (which == OHPIC_RHO || which == OHPIC_PHI) {
+        const void *src = which == OHPIC_RHO ? c->rho : c->phi;
+        if (f64)
+            cudaMemcpyAsync(dst, src, sizeof(double) * g.ncell, cudaMemcpyDeviceToDevice, c->stream);
+        else
+            k_to_double<float><<<blocks_for(g.ncell), 256, 0, c->stream>>>((const float *)src, dst, g.ncell);
+    } else {
+        const int comp = which - OHPIC_EX;
+        if (f64)
+            k_epad_component<dnode><<<blocks_for(g.ncell), 256, 0, c->stream>>>(g, (const dnode *)c->epad, comp, dst);
+        else
+            k_epad_component<float4><<<blocks_for(g.ncell), 256, 0, c->stream>>>(g, (const float4 *)c->epad, comp,
+                                                                                 dst);
+    }
+    ++c->launches;
+}
+
+void field_from_double(ohpic_ctx *c, int which, const double *src)
+{
+    const Geom &g = c->g;
+    const bool f64 = c->cfg.precision == OHPIC_FP64;
+    if (which == OHPIC_RHO || which == OHPIC_PHI) {
+        void *dst = which == OHPIC_RHO ? c->rho : c->phi;
+        if (f64)
+            cudaMemcpyAsync(dst, src, sizeof(double) * g.ncell, cudaMemcpyDeviceToDevice, c->stream);
+        else
+            k_from_double<float><<<blocks_for(g.ncell), 256, 0, c->stream>>>(src, (float *)dst, g.ncell);
+    } else {
+        const int comp = which - OHPIC_EX;
+        if (f64)
+            k_fill_epad<double, dnode><<<blocks_for((int64_t)g.gx * g.gy * g.gz), 256, 0, c->stream>>>(
+                g, src, comp, (dnode *)c->epad);
+        else
+            k_fill_epad<float, float4><<<blocks_for((int64_t)g.gx * g.gy * g.gz), 256, 0, c->stream>>>(
+                g, src, comp, (float4 *)c->epad);
+    }
+    ++c->launches;
+}
+
+}  // namespace ohpic

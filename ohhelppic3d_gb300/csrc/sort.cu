@@ -1,0 +1,234 @@
+// sort.cu -- periodic counting sort of every species by tile-major cell index.
+//
+// No reference counterpart: the reference walks an unsorted oh_particle buffer.
+// The sort makes the particles of one tile a contiguous range so the fused push
+// can stage that tile's fields in shared memory (particles.cu).
+//
+// Per species: histogram of cell keys (global atomics, aggregated per warp with
+// __match_any_sync), exclusive scan of the ncell counters (multi-level block
+// scan), tile start table, then a scatter of every particle array into the
+// second buffer.  Lanes of a warp that share a key take consecutive slots in
+// lane order, so a warp's relative order is kept; order across warps follows
+// the atomic order.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ohpic_internal.cuh"
+
+namespace ohpic {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;                      // per thread
+constexpr int kScanBlock = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t tile_key(const Geom &g, int ix, int iy, int iz)
+{
+    const int tx = ix / g.tx, ty = iy / g.ty, tz = iz / g.tz;
+    const int lx = ix - tx * g.tx, ly = iy - ty * g.ty, lz = iz - tz * g.tz;
+    const uint32_t tile = (uint32_t)tx + (uint32_t)g.ntx * ((uint32_t)ty + (uint32_t)g.nty * (uint32_t)tz);
+    return tile * (uint32_t)g.tile_cells + (uint32_t)lx + (uint32_t)g.tx * ((uint32_t)ly + (uint32_t)g.ty * lz);
+}
+
+template <bool F32>
+__device__ __forceinline__ uint32_t particle_key(const Geom &g, const PartF64 &p64, const PartF32 &p32, int64_t i,
+                                                 DevDiag *d)
+{
+    int ix, iy, iz;
+    if (F32) {
+        const int32_t c = p32.cell[i];
+        ix = cell_x(c); iy = cell_y(c); iz = cell_z(c);
+    } else {
+        ix = (int)p64.x[i]; iy = (int)p64.y[i]; iz = (int)p64.z[i];
+    }
+    if ((unsigned)ix >= (unsigned)g.nx || (unsigned)iy >= (unsigned)g.ny || (unsigned)iz >= (unsigned)g.nz) {
+        if (atomicCAS(&d->err_code, 0, OHPIC_ERR_BOUNDS) == 0) d->err_info = 10;
+        ix = iy = iz = 0;
+    }
+    return tile_key(g, ix, iy, iz);
+}
+
+// Warp-aggregated atomicAdd of 1 per lane on count[key]; returns this lane's slot.
+__device__ __forceinline__ uint32_t aggregated_inc(uint32_t *count, uint32_t key, bool active)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned act = __ballot_sync(kFull, active);
+    const uint32_t k = active ? key : 0xffffffffu - lane;
+    const unsigned peers = __match_any_sync(kFull, k) & act;
+    uint32_t base = 0;
+    const int leader = peers ? __ffs(peers) - 1 : -1;
+    if (active && (int)lane == leader) base = atomicAdd(count + key, (uint32_t)__popc(peers));
+    base = __shfl_sync(kFull, base, leader < 0 ? (int)lane : leader);
+    return base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+}
+
+template <bool F32>
+__global__ void k_hist(Geom g, PartF64 p64, PartF32 p32, int64_t seg, int64_t n, uint32_t *count, DevDiag *d)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += stride) {
+        const int64_t i = base + threadIdx.x;
+        const bool active = i < n;
+        const uint32_t key = active ? particle_key<F32>(g, p64, p32, seg + i, d) : 0u;
+        aggregated_inc(count, key, active);
+    }
+}
+
+template <bool F32>
+__global__ void k_scatter(Geom g, PartF64 s64, PartF32 s32, PartF64 d64, PartF32 d32, const uint32_t *sid,
+                          uint32_t *did, int64_t seg, int64_t n, const uint32_t *start, uint32_t *cursor, DevDiag *d)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += stride) {
+        const int64_t i = base + threadIdx.x;
+        const bool active = i < n;
+        const uint32_t key = active ? particle_key<F32>(g, s64, s32, seg + i, d) : 0u;
+        const uint32_t slot = aggregated_inc(cursor, key, active);
+        if (!active) continue;
+        const int64_t src = seg + i, dst = seg + (int64_t)start[key] + slot;
+        if (F32) {
+            d32.cell[dst] = s32.cell[src];
+            d32.ox[dst] = s32.ox[src]; d32.oy[dst] = s32.oy[src]; d32.oz[dst] = s32.oz[src];
+            d32.vx[dst] = s32.vx[src]; d32.vy[dst] = s32.vy[src]; d32.vz[dst] = s32.vz[src];
+        } else {
+            d64.x[dst] = s64.x[src]; d64.y[dst] = s64.y[src]; d64.z[dst] = s64.z[src];
+            d64.vx[dst] = s64.vx[src]; d64.vy[dst] = s64.vy[src]; d64.vz[dst] = s64.vz[src];
+        }
+        if (sid) did[dst] = sid[src];
+    }
+}
+
+// Exclusive scan of one block of kScanBlock values; block total -> sums[blockIdx].
+__global__ void __launch_bounds__(kScanThreads) k_scan_block(const uint32_t *in, uint32_t *out, int64_t n,
+                                                             uint32_t *sums)
+{
+    __shared__ uint32_t warp_tot[kScanThreads / 32];
+    const int64_t b0 = (int64_t)blockIdx.x * kScanBlock + (int64_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t local = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int64_t i = b0 + k;
+        v[k] = i < n ? in[i] : 0u;
+        local += v[k];
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = local;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warp_tot[lane];
+        uint32_t wi = w;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(kFull, wi, o);
+            if (lane >= o) wi += t;
+        }
+        warp_tot[lane] = wi - w;   // exclusive warp offsets
+        if (lane == 31 && sums) sums[blockIdx.x] = wi;
+    }
+    __syncthreads();
+    uint32_t run = warp_tot[warp] + incl - local;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int64_t i = b0 + k;
+        if (i < n) out[i] = run;
+        run += v[k];
+    }
+}
+
+__global__ void k_add_offsets(uint32_t *out, int64_t n, const uint32_t *offs)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] += offs[i / kScanBlock];
+}
+
+__global__ void k_tile_begin(Geom g, const uint32_t *start, int64_t seg, int64_t count, int64_t *tb)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < g.ntile) tb[t] = seg + (int64_t)start[t * g.tile_cells];
+    if (t == g.ntile) tb[t] = seg + count;
+}
+
+// Exclusive scan of n values (in -> out) using tmp for the block sums of every level.
+void scan_exclusive(ohpic_ctx *c, const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp)
+{
+    const int64_t nb = (n + kScanBlock - 1) / kScanBlock;
+    if (nb <= 1) {
+        k_scan_block<<<1, kScanThreads, 0, c->stream>>>(in, out, n, nullptr);
+        ++c->launches;
+        return;
+    }
+    uint32_t *sums = tmp, *sums_scan = tmp + nb;
+    k_scan_block<<<(unsigned)nb, kScanThreads, 0, c->stream>>>(in, out, n, sums);
+    scan_exclusive(c, sums, sums_scan, nb, tmp + 2 * nb);
+    k_add_offsets<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(out, n, sums_scan);
+    c->launches += 2;
+}
+
+int grid_of(int64_t n)
+{
+    int64_t b = (n + 255) / 256;
+    if (b > 152 * 32) b = 152 * 32;
+    return b < 1 ? 1 : (int)b;
+}
+
+}  // namespace
+
+int64_t scan_tmp_elems(int64_t n)
+{
+    int64_t total = 0;
+    for (int64_t m = n; m > kScanBlock;) {
+        const int64_t nb = (m + kScanBlock - 1) / kScanBlock;
+        total += 2 * nb;
+        m = nb;
+    }
+    return total + 16;
+}
+
+int sort_particles(ohpic_ctx *c)
+{
+    const Geom &g = c->g;
+    const bool f32 = c->cfg.precision == OHPIC_FP32;
+    const int src = c->cur, dst = 1 - c->cur;
+    for (int s = 0; s < c->cfg.nspecies; ++s) {
+        const int64_t n = c->count[s];
+        int64_t *tb = c->tile_begin + (int64_t)s * (g.ntile + 1);
+        cudaMemsetAsync(c->cell_count, 0, sizeof(uint32_t) * g.ncell, c->stream);
+        if (n > 0) {
+            if (f32)
+                k_hist<true><<<grid_of(n), 256, 0, c->stream>>>(g, c->p64[src], c->p32[src], c->seg[s], n,
+                                                                c->cell_count, c->diag);
+            else
+                k_hist<false><<<grid_of(n), 256, 0, c->stream>>>(g, c->p64[src], c->p32[src], c->seg[s], n,
+                                                                 c->cell_count, c->diag);
+            ++c->launches;
+        }
+        scan_exclusive(c, c->cell_count, c->cell_start, g.ncell, c->scan_tmp);
+        k_tile_begin<<<(unsigned)((g.ntile + 1 + 255) / 256), 256, 0, c->stream>>>(g, c->cell_start, c->seg[s], n,
+                                                                                    tb);
+        ++c->launches;
+        if (n > 0) {
+            cudaMemsetAsync(c->cell_count, 0, sizeof(uint32_t) * g.ncell, c->stream);
+            if (f32)
+                k_scatter<true><<<grid_of(n), 256, 0, c->stream>>>(g, c->p64[src], c->p32[src], c->p64[dst],
+                                                                   c->p32[dst], c->ids[src], c->ids[dst], c->seg[s],
+                                                                   n, c->cell_start, c->cell_count, c->diag);
+            else
+                k_scatter<false><<<grid_of(n), 256, 0, c->stream>>>(g, c->p64[src], c->p32[src], c->p64[dst],
+                                                                    c->p32[dst], c->ids[src], c->ids[dst], c->seg[s],
+                                                                    n, c->cell_start, c->cell_count, c->diag);
+            ++c->launches;
+        }
+    }
+    c->cur = dst;
+    c->sorted = true;
+    c->steps_since_sort = 0;
+    return OHPIC_OK;
+}
+
+}  // namespace ohpic

@@ -1,0 +1,336 @@
+"""GPU parity tests: the CUDA path, called through the C ABI, against the oracle.
+
+Tolerances (FP64 plain form):
+  * interp and move in strict mode: bit-exact (same operation order, no FMA).
+  * scatter: atomics change only the summation order of rho: max|diff| <= 1e-13 max|rho|.
+  * solve: cuFFT vs the oracle's FFT: max|diff| <= 1e-12 max|field|.
+  * full steps (fast arithmetic with FMA): particle counts, cell indices and boundary
+    crossings exact; positions/velocities/fields within the bounds in STEP_TOL.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+KEYS = ("x", "y", "z", "vx", "vy", "vz")
+# step -> (max |dx| cells, max |dv|, rel-L2 of rho/phi/E) for the FP64 form
+STEP_TOL = {1: (1e-13, 1e-13, 1e-12), 10: (1e-11, 1e-11, 1e-10), 100: (1e-7, 1e-7, 1e-6)}
+
+
+def _two_species(O, n, ppc=2, weights=0, b0=(0.0, 0.0, 0.5)):
+    return O.Setup(n=n, dt=0.1, b0=b0, weights=weights,
+                   species=[O.SpeciesInit(ppc=ppc, vth=1.0, qm=-1.0, wp=1.0),
+                            O.SpeciesInit(ppc=ppc, vth=0.1, qm=0.01, wp=0.1)])
+
+
+def _config(P, O, setup, caps, precision=0, sort_every=0, tile=(0, 0, 0)):
+    return P.make_config(n=setup.n, dt=setup.dt, b0=setup.b0,
+                         qm=[sp.qm for sp in setup.species],
+                         q=[setup.charge(sp) for sp in setup.species],
+                         capacity=caps, precision=precision, weights=setup.weights,
+                         sort_every=sort_every, tile=tile)
+
+
+def _pair(P, O, setup, precision=0, sort_every=0, tile=(0, 0, 0), threads=8):
+    o = O.Oracle(setup, threads=threads)
+    o.init_particles()
+    caps = [o.count(s) + 64 for s in range(len(setup.species))]
+    ctx = P.PicContext(_config(P, O, setup, caps, precision, sort_every, tile))
+    for s in range(len(setup.species)):
+        ctx.upload(s, o.get_particles(s))
+    return o, ctx
+
+
+def _upload_oracle_E(P, O, o, ctx):
+    for w_o, w_p in ((O.EX, P.EX), (O.EY, P.EY), (O.EZ, P.EZ)):
+        ctx.set_field(w_p, o.get_field(w_o))
+
+
+def _rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_upload_download_roundtrip(ohpic, oracle_mod):
+    P, O = ohpic, oracle_mod
+    setup = _two_species(O, (8, 8, 16))
+    o, ctx = _pair(P, O, setup)
+    for s in range(2):
+        ref = o.get_particles(s)
+        got = ctx.download(s)
+        for k in KEYS:
+            np.testing.assert_array_equal(got[k], ref[k])
+        assert np.array_equal(got["ids"], np.arange(len(ref["x"]), dtype=np.uint32))
+    # AoS records with extra members (the oh_particle layout carries ids after x..vz)
+    ref = o.get_particles(0)
+    rec = np.zeros((len(ref["x"]), 8))
+    for i, k in enumerate(KEYS):
+        rec[:, i] = ref[k]
+    rec[:, 6] = 123.0
+    ctx.upload_aos(0, rec)
+    back = ctx.download_aos(0, width=8)
+    np.testing.assert_array_equal(back[:, :6], rec[:, :6])
+    ctx.close()
+
+
+def test_upload_fp32_form_roundtrip(ohpic, oracle_mod):
+    """FP32 form: cell index exact, offset rounded to FP32 (|err| <= 2^-24)."""
+    P, O = ohpic, oracle_mod
+    setup = _two_species(O, (8, 8, 16))
+    o, ctx = _pair(P, O, setup, precision=P.FP32)
+    for s in range(2):
+        ref = o.get_particles(s)
+        got = ctx.download(s)
+        for k in ("x", "y", "z"):
+            assert np.max(np.abs(got[k] - ref[k])) <= 2.0 ** -24 * 1.0001
+        for k in ("vx", "vy", "vz"):
+            assert np.max(np.abs(got[k] - ref[k]) / np.maximum(np.abs(ref[k]), 1e-30)) <= 2.0 ** -24
+    ctx.close()
+
+
+@pytest.mark.parametrize("weights", [0, 1])
+@pytest.mark.parametrize("sorted_", [False, True])
+def test_interp_strict_bitexact(ohpic, oracle_mod, weights, sorted_):
+    """t_Interpolator%interp: same nodes, same weights, same summation order."""
+    P, O = ohpic, oracle_mod
+    setup = _two_species(O, (8, 16, 8), weights=weights)
+    o, ctx = _pair(P, O, setup, tile=(4, 4, 4))
+    o.deposit()
+    o.solve()
+    if sorted_:
+        ctx.sort()
+    _upload_oracle_E(P, O, o, ctx)
+    for s in range(2):
+        e = ctx.interp(s)
+        dev = ctx.download(s, order=False)
+        ids = dev["ids"]
+        ref = o.get_particles(s)
+        exp = np.array([o.interp(ref["x"][i], ref["y"][i], ref["z"][i]) for i in ids])
+        np.testing.assert_array_equal(e, exp)
+    ctx.close()
+
+
+@pytest.mark.parametrize("weights", [0, 1])
+@pytest.mark.parametrize("sorted_", [False, True])
+def test_move_strict_bitexact(ohpic, oracle_mod, weights, sorted_):
+    """t_ParticleMover%move + apply x2 in strict FP64: bit-identical to the oracle."""
+    P, O = ohpic, oracle_mod
+    setup = _two_species(O, (16, 8, 8), weights=weights)
+    o, ctx = _pair(P, O, setup, tile=(4, 4, 4))
+    o.deposit()
+    o.solve()
+    if sorted_:
+        ctx.sort()
+    _upload_oracle_E(P, O, o, ctx)
+    ctx.move(setup.dt)
+    o.push()
+    for s in range(2):
+        got, ref = ctx.download(s), o.get_particles(s)
+        for k in KEYS:
+            np.testing.assert_array_equal(got[k], ref[k])
+    d_gpu, d_orc = ctx.diagnostics(), o.diagnostics()
+    assert d_gpu["crossings"] == d_orc["crossings"]
+    ctx.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("sorted_", [False, True])
+def test_scatter_matches_oracle(ohpic, oracle_mod, precision, sorted_):
+    P, O = ohpic, oracle_mod
+    setup = _two_species(O, (16, 16, 8), ppc=4)
+    o, ctx = _pair(P, O, setup, precision=precision, tile=(4, 8, 4))
+    if sorted_:
+        ctx.sort()
+    ctx.scatter()
+    o.deposit()
+    got, ref = ctx.field(P.RHO), o.get_field(O.RHO)
+    scale = np.max(np.abs(ref))
+    if precision == 0:
+        assert np.max(np.abs(got - ref)) <= 1e-13 * scale
+    else:
+        assert np.max(np.abs(got - ref)) <= 2e-6 * scale
+    assert abs(got.sum() - ref.sum()) <= (1e-12 if precision == 0 else 1e-4) * np.abs(ref).sum()
+    ctx.close()
+
+
+@pytest.mark.parametrize("n", [(8, 8, 8), (16, 12, 24), (32, 32, 32)])
+def test_solve_matches_oracle(ohpic, oracle_mod, n):
+    """t_FieldSolver%solve from an identical rho: cuFFT against the oracle's FFT."""
+    P, O = ohpic, oracle_mod
+    setup = _two_species(O, n, ppc=1)
+    o, ctx = _pair(P, O, setup)
+    o.deposit()
+    o.solve()
+    ctx.set_field(P.RHO, o.get_field(O.RHO))
+    ctx.solve()
+    for wp, wo in ((P.PHI, O.PHI), (P.EX, O.EX), (P.EY, O.EY), (P.EZ, O.EZ)):
+        got, ref = ctx.field(wp), o.get_field(wo)
+        assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref)), wp
+    # the reference t_OhField layout (values(1:6, -1:n+2, ...)) with periodic halos
+    eb = ctx.field_ohfield(P.EX, (-1, -1, -1), (n[0] + 2, n[1] + 2, n[2] + 2), 6)
+    ex = ctx.field(P.EX)
+    assert eb[1, 1, 1, 0] == ex[0, 0, 0]
+    assert eb[0, 1, 1, 0] == ex[0, 0, n[0] - 1]           # x = -1 is the periodic image of n-1
+    assert eb[1, 1, n[0] + 1, 0] == ex[0, 0, 0]             # x = n is node 0
+    assert np.all(eb[..., 5] == setup.b0[2])
+    ctx.close()
+
+
+def _cells(p, n):
+    return np.stack([np.floor(p["x"]), np.floor(p["y"]), np.floor(p["z"])]).astype(np.int64)
+
+
+def _compare_state(P, O, o, ctx, setup, step, report):
+    o.deposit()
+    o.solve()
+    ctx.solve()
+    tol_x, tol_v, tol_f = STEP_TOL[step]
+    for s in range(len(setup.species)):
+        got, ref = ctx.download(s), o.get_particles(s)
+        assert len(got["x"]) == len(ref["x"])
+        mism = int(np.sum(np.any(_cells(got, setup.n) != _cells(ref, setup.n), axis=0)))
+        dx = max(float(np.max(np.abs(got[k] - ref[k]))) for k in ("x", "y", "z"))
+        dv = max(float(np.max(np.abs(got[k] - ref[k]))) for k in ("vx", "vy", "vz"))
+        report.append((step, s, mism, dx, dv))
+        assert mism == 0, (step, s, mism)
+        assert dx <= tol_x and dv <= tol_v, (step, s, dx, dv)
+    for wp, wo in ((P.RHO, O.RHO), (P.PHI, O.PHI), (P.EX, O.EX), (P.EY, O.EY), (P.EZ, O.EZ)):
+        err = _rel_l2(ctx.field(wp), o.get_field(wo))
+        report.append((step, "field", wp, err))
+        assert err <= tol_f, (step, wp, err)
+
+
+@pytest.mark.parametrize("sort_every", [0, 20])
+def test_step_parity_fp64_c1(ohpic, oracle_mod, sort_every):
+    """The 32^3, 2 x 16 ppc plain-FP64 configuration after 1, 10 and 100 steps."""
+    P, O = ohpic, oracle_mod
+    setup = _two_species(O, (32, 32, 32), ppc=16)
+    o, ctx = _pair(P, O, setup, sort_every=sort_every, threads=16)
+    d0 = ctx.diagnostics()
+    report = []
+    done = 0
+    for step in (1, 10, 100):
+        ctx.step(setup.dt, step - done)
+        o.step(step - done)
+        done = step
+        crossings_gpu = ctx.diagnostics()["crossings"]
+        crossings_orc = o.diagnostics()["crossings"]
+        assert crossings_gpu == crossings_orc, (step, crossings_gpu, crossings_orc)
+        _compare_state(P, O, o, ctx, setup, step, report)
+    d1 = ctx.diagnostics()
+    assert d1["count"] == d0["count"]
+    assert abs(d1["total_charge"]) < 1e-9
+    e0 = d0["kinetic_energy"] + d0["field_energy"]
+    e1 = d1["kinetic_energy"] + d1["field_energy"]
+    do = o.diagnostics()
+    assert abs(e1 - (do["kinetic_energy"] + do["field_energy"])) <= 1e-9 * e0
+    print("parity report", report, "energy drift", (e1 - e0) / e0)
+    ctx.close()
+
+
+def test_fp32_form_against_fp64_oracle(ohpic, oracle_mod):
+    """Precision form on the 32^3 configuration: field errors against the FP64 oracle."""
+    P, O = ohpic, oracle_mod
+    setup = _two_species(O, (32, 32, 32), ppc=16)
+    o, ctx = _pair(P, O, setup, precision=P.FP32, sort_every=20, threads=16)
+    done = 0
+    errs = {}
+    for step in (1, 10, 100):
+        ctx.step(setup.dt, step - done)
+        o.step(step - done)
+        done = step
+        o.deposit()
+        o.solve()
+        ctx.solve()
+        errs[step] = {name: _rel_l2(ctx.field(wp), o.get_field(wo))
+                      for name, wp, wo in (("rho", P.RHO, O.RHO), ("phi", P.PHI, O.PHI),
+                                           ("ex", P.EX, O.EX), ("ey", P.EY, O.EY), ("ez", P.EZ, O.EZ))}
+        for s in range(2):
+            assert ctx.count(s) == o.count(s)
+    print("fp32 form rel-L2 errors", errs)
+    assert errs[1]["ex"] < 1e-5 and errs[1]["rho"] < 1e-5
+    assert errs[10]["ex"] < 1e-4
+    assert errs[100]["ex"] < 1e-1
+    ctx.close()
+
+
+def test_sort_invariants(ohpic, oracle_mod):
+    P, O = ohpic, oracle_mod
+    setup = _two_species(O, (16, 16, 16), ppc=2)
+    for precision in (0, 1):
+        o, ctx = _pair(P, O, setup, precision=precision, tile=(8, 4, 8))
+        before = [ctx.download(s) for s in range(2)]
+        ctx.sort()
+        for s in range(2):
+            dev = ctx.download(s, order=False)
+            ids = dev["ids"]
+            assert np.array_equal(np.sort(ids), np.arange(len(ids), dtype=np.uint32))
+            cx, cy, cz = (np.floor(dev[k]).astype(np.int64) for k in ("x", "y", "z"))
+            t = (cx // 8) + 2 * ((cy // 4) + 4 * (cz // 8))
+            key = t * 256 + (cx % 8) + 8 * ((cy % 4) + 4 * (cz % 8))
+            assert np.all(np.diff(key) >= 0)
+            back = ctx.download(s)
+            for k in KEYS:
+                np.testing.assert_array_equal(back[k], before[s][k])
+        ctx.close()
+
+
+def test_edge_positions_and_empty_species(ohpic, oracle_mod):
+    """Particles on cell faces, at 0 and just below n, an empty species, and the
+    rounding case where n + p rounds to n (wrapped to 0 by the second apply)."""
+    P, O = ohpic, oracle_mod
+    n = (8, 8, 8)
+    setup = O.Setup(n=n, dt=0.1, b0=(0.0, 0.0, 0.5),
+                    species=[O.SpeciesInit(ppc=1, vth=1.0, qm=-1.0, q=-0.1),
+                             O.SpeciesInit(ppc=1, vth=0.1, qm=0.01, q=0.1)])
+    xs = np.array([0.0, 7.999999999999999, 4.0, 1e-300, 3.5, 0.0, 5.0])
+    vs = np.array([-1e-15, 1.0, 0.0, -1e-290, 0.25, -2.0, 10.0])
+    p = {"x": xs, "y": xs[::-1].copy(), "z": np.full(len(xs), 2.0),
+         "vx": vs, "vy": -vs, "vz": np.zeros(len(xs))}
+    o = O.Oracle(setup, capacity=[16, 16])
+    o.set_particles(0, p)
+    o.set_particles(1, {k: np.zeros(0) for k in KEYS})
+    ctx = P.PicContext(_config(P, O, setup, [16, 16]))
+    ctx.upload(0, p)
+    ctx.upload(1, {k: np.zeros(0) for k in KEYS})
+    o.deposit()
+    o.solve()
+    _upload_oracle_E(P, O, o, ctx)
+    ctx.move(0.1)
+    o.push()
+    got, ref = ctx.download(0), o.get_particles(0)
+    for k in KEYS:
+        np.testing.assert_array_equal(got[k], ref[k])
+    assert np.all((got["x"] >= 0) & (got["x"] < 8))
+    assert ctx.count(1) == 0
+    ctx.step(0.1, 3)
+    assert ctx.count(0) == len(xs)
+    ctx.close()
+
+
+def test_errors_are_status_codes(ohpic, oracle_mod):
+    P, O = ohpic, oracle_mod
+    setup = _two_species(O, (8, 8, 8), ppc=1)
+    ctx = P.PicContext(_config(P, O, setup, [4, 4]))
+    with pytest.raises(P.OhpicError) as e:
+        ctx.upload(0, {k: np.zeros(5) for k in KEYS})
+    assert e.value.status == P.ERR_CAPACITY
+    with pytest.raises(P.OhpicError) as e:
+        ctx.upload(2, {k: np.zeros(1) for k in KEYS})
+    assert e.value.status == P.ERR_INVALID
+    L = P.lib()
+    assert L.ohpic_move_one(ctx.ptr, None, 1.0, None, 0.1) == P.ERR_UNSUPPORTED
+    assert L.ohpic_scatter_one(ctx.ptr, None, 1.0, 1) == P.ERR_UNSUPPORTED
+    # an out-of-grid position is caught by the kernel's bounds check, not a fault
+    bad = {k: np.zeros(2) for k in KEYS}
+    bad["x"] = np.array([1.0, 99.0])
+    ctx.upload(0, bad)
+    with pytest.raises(P.OhpicError) as e:
+        ctx.scatter()
+        ctx.synchronize()
+    assert e.value.status == P.ERR_BOUNDS
+    ctx.upload(0, {k: np.ones(2) for k in KEYS})
+    ctx.scatter()
+    ctx.synchronize()
+    ctx.close()
