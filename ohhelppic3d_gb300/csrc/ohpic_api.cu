@@ -454,8 +454,8 @@ int ohpic_interp(ohpic_ctx *c, int s, double *e_out, int64_t capacity, int64_t *
         const int rc = do_solve(c);
         if (rc != OHPIC_OK) return rc;
     }
-    int64_t need = 0;
-    for (int k = 0; k < c->cfg.nspecies; ++k) need = std::max<int64_t>(need, 3 * c->count[k]);
+    // One slot of 3 doubles per particle slot of every species (absolute index).
+    const int64_t need = 3 * c->total_slots;
     if (need > c->interp_cap) {
         dfree(c->interp_buf);
         c->interp_buf = nullptr;
@@ -467,8 +467,8 @@ int ohpic_interp(ohpic_ctx *c, int s, double *e_out, int64_t capacity, int64_t *
     const int strict = 1;
     launch_tiled(c, MODE_INTERP, strict);
     if (n > 0)
-        OHPIC_CUDA_TRY(c, cudaMemcpyAsync(e_out, c->interp_buf, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost,
-                                          c->stream));
+        OHPIC_CUDA_TRY(c, cudaMemcpyAsync(e_out, c->interp_buf + 3 * c->seg[s], sizeof(double) * 3 * n,
+                                          cudaMemcpyDeviceToHost, c->stream));
     return check_device(c);
 }
 

@@ -105,7 +105,7 @@ struct TileArgs {
     const int64_t *tile_begin;         // [nspecies][ntile+1], absolute array indices
     const void *epad;                  // padded E
     void *rho;                         // n^3 (zeroed by the caller for deposit modes)
-    double *interp_out;                // MODE_INTERP: 3 per particle (species-relative)
+    double *interp_out;                // MODE_INTERP: 3 per particle slot (absolute index)
     DevDiag *diag;
     int chunk;                         // particles per CTA when unsorted
 };

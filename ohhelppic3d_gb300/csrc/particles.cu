@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(256) tiled_f64(TileArgs a, PartF64 p)
                     }
                 }
                 if (MODE == MODE_INTERP) {
-                    double *o = a.interp_out + 3 * (i0 + j - a.seg[sp]);
+                    double *o = a.interp_out + 3 * (i0 + j);
                     o[0] = ex;
                     o[1] = ey;
                     o[2] = ez;
@@ -623,7 +623,7 @@ __global__ void __launch_bounds__(256) tiled_f32(TileArgs a, PartF32 p)
                     ez = fmaf(nd[n].z, ww[n], ez);
                 }
                 if (MODE == MODE_INTERP) {
-                    double *o = a.interp_out + 3 * (i0 + j - a.seg[sp]);
+                    double *o = a.interp_out + 3 * (i0 + j);
                     o[0] = ex;
                     o[1] = ey;
                     o[2] = ez;
