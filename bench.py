@@ -1,0 +1,410 @@
+"""Benchmark of the particle hot path: particle-steps/s on one GB300 (or N replicas).
+
+Default workload: the 256^3 configuration (2 species x 32 ppc = 1,073,741,824
+particles), run in the FP32 precision form (headline `value`) and the plain
+FP64 form (`fp64_form`).  A step is one mainstep: spectral field solve, then
+the fused gather + Boris + periodic wrap + deposit over every particle; the
+cell sort runs every 20 steps counted from the first timed step (so a timed
+region of K <= 20 steps always contains one sort).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload c2|c1|c4] [--forms fp32,fp64] [--no-e2e] [--no-cpu-baseline]
+
+For N > 1 (launched with torch.distributed.run) every rank advances its own
+replica of the workload (different random streams); there is no collective on
+the data path ("replicas only"), only a barrier and a max-reduction of the
+timings.  `--impl reference` times the reference's CPU path (the C restatement
+in oracle/, since the Fortran reference cannot be built) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s (1 GB300, %HBM peak), FP32 vs FP64; ensemble p50/p99 latency"
+UNIT = "particle-steps/s"
+# Algorithmic bytes of the fused push kernel per particle (one read + one write of
+# the record) and per grid node (E read + rho write), by form.
+PUSH_BYTES_PER_PARTICLE = {"fp32": 2 * (4 + 12 + 12), "fp64": 2 * 48}
+PUSH_BYTES_PER_NODE = {"fp32": 12 + 4, "fp64": 24 + 8}
+# Whole-step grid term: rho write, R2C read, spectrum write, scale r/w, C2R read,
+# phi write, stencil read, E write, gather read (per node).
+STEP_BYTES_PER_NODE = {"fp32": 72, "fp64": 144}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during timed regions."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "50", "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            time.sleep(0.12)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            if self.thread:
+                self.thread.join(timeout=2)
+            self.proc = None
+
+    def summary(self) -> dict:
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return None
+        sm = sorted(x for x in (num(r[1]) for r in self.rows) if x is not None)
+        mx = [x for x in (num(r[2]) for r in self.rows) if x is not None]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[i - 5] for r in self.rows for i in range(5, 9) if r[i].lower().startswith("active")})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------------------
+# Distributed plumbing (replicas only)
+# ---------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = False
+
+    def init(self):
+        import torch
+        import torch.distributed as dist
+        if self.world > 1 and not dist.is_initialized():
+            dist.init_process_group("nccl", device_id=torch.device("cuda", self.local))
+            self.pg = True
+
+    def barrier(self):
+        if self.pg:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def make_context(P, wl, form: str, weights: int, device: int):
+    caps = [c + 1024 for c in wl.counts()]
+    cfg = P.make_config(n=wl.n, dt=wl.dt, b0=wl.b0, qm=[s.qm for s in wl.species], q=[s.q for s in wl.species],
+                        capacity=caps, precision=P.FP32 if form == "fp32" else P.FP64, weights=weights,
+                        sort_every=0, device=device)
+    return P.PicContext(cfg)
+
+
+def species_inits(P, wl):
+    return [P.species_init(s.ppc, s.vth, s.drift, s.lo, s.hi if s.hi is not None else (1e30, 1e30, 1e30))
+            for s in wl.species]
+
+
+def timed_steps(ctx, wl, k: int, on_step=None):
+    for i in range(k):
+        if wl.sort_every and i % wl.sort_every == 0:
+            ctx.sort()
+        ctx.step(wl.dt, 1)
+        if on_step is not None:
+            on_step()
+
+
+def run_form(P, torch, dist, wl, form, args, sampler, peak):
+    ctx = make_context(P, wl, form, args.weights, dist.local)
+    counts = ctx.init_particles(species_inits(P, wl), seed=(42, 52 + dist.rank))
+    n_local = sum(counts)
+    ctx.sort()
+    for _ in range(args.warmup):
+        ctx.step(wl.dt, 1)
+    ctx.synchronize()
+    ctx.set_push_timing(True)
+    launches0 = ctx.stats()["launches"]
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    e0.record(stream)
+    timed_steps(ctx, wl, args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    sampler.stop()
+    dist.barrier()
+    ms = e0.elapsed_time(e1)
+    st = ctx.stats()
+    ms_max = dist.max(ms)
+    n_total = dist.sum(float(n_local))
+    value = n_total * args.steps / (ms_max / 1e3)
+    avg_push_ms = st["push_ms"] / max(st["push_launches"], 1)
+    push_bytes = n_local * PUSH_BYTES_PER_PARTICLE[form] + wl.ncell * PUSH_BYTES_PER_NODE[form]
+    achieved = push_bytes / (avg_push_ms / 1e3) / 1e9
+    step_bytes = n_local * PUSH_BYTES_PER_PARTICLE[form] + wl.ncell * STEP_BYTES_PER_NODE[form]
+    out = {
+        "value": value, "ms_per_step": ms_max / args.steps, "particles": int(n_total),
+        "roofline": {"bound": "hbm", "kernel": f"tiled_{'f32' if form == 'fp32' else 'f64'}<MODE_PUSH> (fused push)",
+                     "achieved": achieved, "peak": peak[0], "unit": "GB/s", "frac": achieved / peak[0],
+                     "traffic": None, "bytes_per_launch": push_bytes, "avg_launch_ms": avg_push_ms,
+                     "peak_source": peak[1]},
+        "step_hbm_frac": step_bytes / (ms_max / args.steps / 1e3) / 1e9 / peak[0],
+        "push_share": st["push_ms"] / ms if ms > 0 else None,
+        "gpu_launches": st["launches"] - launches0,
+    }
+    return ctx, counts, out
+
+
+def run_e2e(P, torch, dist, wl, form, args, ctx, counts):
+    """The same K steps through the C ABI with host buffers: upload every particle
+    from pinned host memory, K steps each followed by a diagnostics read (the
+    step's result: charge and energies), and a download of every particle."""
+    import numpy as np
+    host = []
+    for s, n in enumerate(counts):
+        arrs = {k: torch.empty(max(n, 1), dtype=torch.float64, pin_memory=True).numpy()
+                for k in ("x", "y", "z", "vx", "vy", "vz")}
+        ctx.download_into(s, arrs)
+        host.append(arrs)
+    ctx.set_energy_tracking(True)
+    ctx.synchronize()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for s, n in enumerate(counts):
+        ctx.upload_n(s, host[s], n)
+    timed_steps(ctx, wl, args.steps, on_step=ctx.diagnostics)
+    for s in range(len(counts)):
+        ctx.download_into(s, host[s])
+    ctx.synchronize()
+    t1 = time.perf_counter()
+    dist.barrier()
+    sec = dist.max(t1 - t0)
+    n_total = dist.sum(float(sum(counts)))
+    moved = 48 * sum(counts)
+    finite = bool(np.isfinite(host[0]["x"][:1000]).all())
+    return {"value": n_total * args.steps / sec, "unit": UNIT,
+            "h2d_bytes_per_step": moved / args.steps,
+            "d2h_bytes_per_step": (moved + args.steps * 160) / args.steps,
+            "seconds": sec, "finite": finite,
+            "how": ("job through the C ABI: ohpic_upload_particles_soa from pinned FP64 host arrays, "
+                    "K x (ohpic_step + ohpic_diagnostics), ohpic_download_particles_soa")}
+
+
+# ---------------------------------------------------------------------------
+# CPU path (oracle): the reference's algorithm on the host cores
+# ---------------------------------------------------------------------------
+def cpu_sample_step(wl, fraction: float, threads: int, weights: int, steps: int = 1):
+    """Times `steps` mainsteps of the oracle on `fraction` of the workload's
+    particles (full grid), returning the extrapolated full-workload seconds per step."""
+    import oracle as O
+    species = [O.SpeciesInit(ppc=s.ppc * fraction, vth=s.vth, qm=s.qm, q=s.q, drift=s.drift, lo=s.lo, hi=s.hi)
+               for s in wl.species]
+    setup = O.Setup(n=wl.n, dt=wl.dt, b0=wl.b0, species=species, weights=weights)
+    o = O.Oracle(setup, threads=threads)
+    o.init_particles()
+    n_sample = sum(o.count(i) for i in range(len(species)))
+    per_step = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        o.deposit()
+        t1 = time.perf_counter()
+        o.solve()
+        t2 = time.perf_counter()
+        o.push()
+        t3 = time.perf_counter()
+        t_particles = (t1 - t0) + (t3 - t2)
+        per_step.append(t_particles * wl.nparticles / n_sample + (t2 - t1))
+    o.close()
+    return per_step, n_sample
+
+
+def cpu_sample_fraction(wl) -> float:
+    # about 6.7e7 sampled particles at 256^3; the whole workload when it is small
+    return min(1.0, 6.7e7 / max(wl.nparticles, 1))
+
+
+def run_reference(args, wl):
+    dist = Dist()
+    if dist.rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    frac = cpu_sample_fraction(wl)
+    warm, _ = cpu_sample_step(wl, frac, threads, args.weights, steps=max(args.warmup, 0) and 1)
+    times, n_sample = cpu_sample_step(wl, frac, threads, args.weights, steps=args.steps)
+    sec = sum(times)
+    value = wl.nparticles * args.steps / sec
+    sample = (f"{args.steps} mainsteps (deposit + FFT solve + push) of the oracle on {n_sample} of the "
+              f"{wl.nparticles} particles (uniform over the full {wl.n[0]}x{wl.n[1]}x{wl.n[2]} grid); "
+              f"particle time scaled to the full count, field solve counted once per step")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+        "data": "synthetic: pcg32 seeds (42, 52), the reference injector's draw order",
+        "config": {"workload": wl.description, "form": "reference CPU path (FP64)", "weights": _wname(args.weights)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _wname(w: int) -> str:
+    return "reference (swapped CIC, linear_scatter.f90:41-52)" if w == 0 else "standard CIC"
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c4"])
+    ap.add_argument("--forms", default="fp32,fp64")
+    ap.add_argument("--weights", type=int, default=0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n", default=None, help="grid override nx,ny,nz (same physics and ppc; for profiling)")
+    args = ap.parse_args(argv)
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+
+    from ohhelppic3d_gb300.workloads import WORKLOADS
+    wl = WORKLOADS[args.workload]()
+    if args.n:
+        wl.n = tuple(int(v) for v in args.n.split(","))
+        wl.description += f" [grid overridden to {wl.n[0]}x{wl.n[1]}x{wl.n[2]}]"
+    if args.impl == "reference":
+        return run_reference(args, wl)
+
+    import torch
+
+    import ohhelppic3d_gb300 as P
+    dist = Dist()
+    torch.cuda.set_device(dist.local)
+    dist.init()
+    peak = _peaks()
+    forms = [f.strip() for f in args.forms.split(",") if f.strip()]
+    sampler = ClockSampler(dist.local)
+    results = {}
+    e2e = None
+    for i, form in enumerate(forms):
+        ctx, counts, res = run_form(P, torch, dist, wl, form, args, sampler, peak)
+        if i == 0 and not args.no_e2e:
+            e2e = run_e2e(P, torch, dist, wl, form, args, ctx, counts)
+        ctx.close()
+        torch.cuda.empty_cache()
+        results[form] = res
+
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        frac = cpu_sample_fraction(wl)
+        times, n_sample = cpu_sample_step(wl, frac, threads, args.weights, steps=2)
+        sec = times[-1]
+        cpu = {"value": wl.nparticles / sec, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": (f"1 timed mainstep (after 1 untimed) of the oracle on {n_sample} of {wl.nparticles} "
+                          f"particles over the full grid; particle time scaled to the full count, field solve once")}
+
+    head = forms[0]
+    r = results[head]
+    line = {
+        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if head == "fp32" else "f64",
+        "data": "synthetic: device-side pcg32 injector, seeds (42, 52 + rank), Maxwellian velocities",
+        "config": {"workload": wl.description, "form": {"fp32": "FP32 precision form (int32 cell + FP32 offset)",
+                                                        "fp64": "plain FP64 form"}[head],
+                   "weights": _wname(args.weights), "particles": r["particles"],
+                   "l2": "inputs larger than L2 (particle state >= 30 GB per GPU)",
+                   "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU"},
+        "roofline": r["roofline"],
+        "step_hbm_frac": r["step_hbm_frac"],
+        "gpu_launches": r["gpu_launches"],
+        "clocks": sampler.summary(),
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    for form, res in results.items():
+        if form != head:
+            line[f"{form}_form"] = {"value": res["value"], "ms_per_step": res["ms_per_step"],
+                                   "dtype": "f64" if form == "fp64" else "f32", "roofline": res["roofline"],
+                                   "step_hbm_frac": res["step_hbm_frac"], "gpu_launches": res["gpu_launches"]}
+    if "fp64" in results and head == "fp32":
+        line["fp32_over_fp64"] = results["fp32"]["value"] / results["fp64"]["value"]
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

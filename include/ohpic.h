@@ -98,6 +98,15 @@ typedef struct ohpic_diag {
     double momentum[3];         /* sum (q/qm) v */
 } ohpic_diag;
 
+/* Injector parameters of one species (src/particle_injector/particle_injector_manager.f90:55-70
+ * with the Maxwellian enabled, sigma = vth). */
+typedef struct ohpic_species_init {
+    double ppc;                 /* macro-particles per cell inside the range */
+    double vth;                 /* Maxwellian standard deviation; clipped at +-6 vth */
+    double drift[3];            /* added after the clip (beams) */
+    double lo[3], hi[3];        /* position range, clipped to [0, n] */
+} ohpic_species_init;
+
 typedef struct ohpic_ctx ohpic_ctx;
 
 /* Fills cfg with defaults (FP64 form, reference weights, sort every 20 steps,
@@ -121,6 +130,17 @@ int ohpic_upload_particles(ohpic_ctx *ctx, int species, const void *pbuf, int64_
 int ohpic_upload_particles_soa(ohpic_ctx *ctx, int species, const double *x, const double *y,
                                const double *z, const double *vx, const double *vy,
                                const double *vz, int64_t n);
+/* Device-side initial conditions with the reference injector's random streams:
+ * PCG32 seeded (initstate, initseq) and advanced by `advance`
+ * (src/ohhelppic3d.f90:111-112), then per species one random_fix draw
+ * (src/radom/random_generator.f90:45-58) and 7 draws per particle (x, y, z,
+ * then the 4-draw Maxwellian; particle_injector_with_distribution.f90:51-69).
+ * Positions are bit-identical to the reference injector fed the same streams;
+ * velocities use the device libm.  counts_out (nullable) receives the
+ * per-species counts.  Replaces initialize_particles (particle_injector_manager.f90:88-98). */
+int ohpic_init_particles(ohpic_ctx *ctx, uint64_t initstate, uint64_t initseq, uint64_t advance,
+                         const ohpic_species_init *species, int64_t *counts_out);
+
 /* Download in device order; ids (nullable) receive each particle's index in
  * the last upload, so a caller can restore its own order. */
 int ohpic_download_particles_soa(ohpic_ctx *ctx, int species, double *x, double *y, double *z,
@@ -173,6 +193,10 @@ int ohpic_download_field_ohfield(ohpic_ctx *ctx, int which, double *values, int 
                                  const int32_t lo[3], const int32_t hi[3]);
 
 int ohpic_diagnostics(ohpic_ctx *ctx, ohpic_diag *out);
+/* With tracking on, the fused push also sums |v|^2 and v per species, so a
+ * per-step ohpic_diagnostics reads them instead of making a second pass over
+ * the particles. */
+int ohpic_set_energy_tracking(ohpic_ctx *ctx, int enable);
 
 /* The per-particle bindings of the reference cannot be served from device
  * memory; the batched calls above replace them.  These return

@@ -55,6 +55,21 @@ class Diag(C.Structure):
     ]
 
 
+class SpeciesInit(C.Structure):
+    _fields_ = [
+        ("ppc", C.c_double), ("vth", C.c_double), ("drift", C.c_double * 3),
+        ("lo", C.c_double * 3), ("hi", C.c_double * 3),
+    ]
+
+
+def species_init(ppc, vth, drift=(0.0, 0.0, 0.0), lo=(0.0, 0.0, 0.0), hi=(1e30, 1e30, 1e30)) -> SpeciesInit:
+    s = SpeciesInit()
+    s.ppc, s.vth = float(ppc), float(vth)
+    for d in range(3):
+        s.drift[d], s.lo[d], s.hi[d] = float(drift[d]), float(lo[d]), float(hi[d])
+    return s
+
+
 class OhpicError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"ohpic status {status}: {message}")
@@ -70,6 +85,8 @@ SIGNATURES = {
     "ohpic_config_default": (None, [C.POINTER(Config)]),
     "ohpic_create": (C.c_int, [C.POINTER(Config), C.POINTER(_P)]),
     "ohpic_destroy": (C.c_int, [_P]),
+    "ohpic_init_particles": (C.c_int, [_P, C.c_uint64, C.c_uint64, C.c_uint64, C.POINTER(SpeciesInit),
+                                       C.POINTER(C.c_int64)]),
     "ohpic_upload_particles": (C.c_int, [_P, C.c_int, _P, C.c_int64, C.c_int64]),
     "ohpic_upload_particles_soa": (C.c_int, [_P, C.c_int] + [_DP] * 6 + [C.c_int64]),
     "ohpic_download_particles_soa": (C.c_int, [_P, C.c_int] + [_DP] * 6 +
@@ -87,6 +104,7 @@ SIGNATURES = {
     "ohpic_download_field_ohfield": (C.c_int, [_P, C.c_int, _DP, C.c_int,
                                                C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "ohpic_diagnostics": (C.c_int, [_P, C.POINTER(Diag)]),
+    "ohpic_set_energy_tracking": (C.c_int, [_P, C.c_int]),
     "ohpic_move_one": (C.c_int, [_P, _DP, C.c_double, _DP, C.c_double]),
     "ohpic_scatter_one": (C.c_int, [_P, _DP, C.c_double, C.c_int]),
     "ohpic_last_error": (C.c_int, [_P, C.c_char_p, C.c_size_t]),
@@ -194,6 +212,13 @@ class PicContext:
         return s.value or 0
 
     # -- particles --------------------------------------------------------
+    def init_particles(self, species: list, seed=(42, 52), advance: int = 0) -> list:
+        """Device-side injector (reference streams); species: list of SpeciesInit."""
+        arr = (SpeciesInit * max(len(species), 1))(*species)
+        counts = (C.c_int64 * MAX_SPECIES)()
+        self._check(lib().ohpic_init_particles(self.ptr, seed[0], seed[1], advance % (1 << 64), arr, counts))
+        return [counts[i] for i in range(self.nspecies)]
+
     def upload(self, species: int, p: dict):
         arrs = [np.ascontiguousarray(p[k], dtype=np.float64) for k in ("x", "y", "z", "vx", "vy", "vz")]
         self._check(lib().ohpic_upload_particles_soa(self.ptr, species, *[_dp(a) for a in arrs], len(arrs[0])))
@@ -224,6 +249,20 @@ class PicContext:
                 perm = np.argsort(res["ids"], kind="stable")
                 res = {k: v[perm] for k, v in res.items()}
         return res
+
+    def download_into(self, species: int, out: dict, ids: np.ndarray | None = None) -> int:
+        """Device-order download into caller-provided float64 arrays (e.g. pinned host memory)."""
+        cap = min(len(out[k]) for k in ("x", "y", "z", "vx", "vy", "vz"))
+        n = C.c_int64()
+        self._check(lib().ohpic_download_particles_soa(
+            self.ptr, species, *[_dp(out[k]) for k in ("x", "y", "z", "vx", "vy", "vz")],
+            ids.ctypes.data_as(C.POINTER(C.c_uint32)) if ids is not None else None, cap, C.byref(n)))
+        return n.value
+
+    def upload_n(self, species: int, p: dict, n: int):
+        """Upload the first n particles of caller-provided float64 arrays (no copy on the host)."""
+        self._check(lib().ohpic_upload_particles_soa(
+            self.ptr, species, *[_dp(p[k]) for k in ("x", "y", "z", "vx", "vy", "vz")], n))
 
     def download_aos(self, species: int, width: int = 6) -> np.ndarray:
         cap = int(self.cfg.capacity[species])
@@ -294,6 +333,9 @@ class PicContext:
             "kinetic_energy": d.kinetic_energy,
             "momentum": [d.momentum[i] for i in range(3)],
         }
+
+    def set_energy_tracking(self, on: bool):
+        self._check(lib().ohpic_set_energy_tracking(self.ptr, 1 if on else 0))
 
     # -- instrumentation ------------------------------------------------------
     def set_push_timing(self, on: bool):

@@ -120,7 +120,9 @@ int do_solve(ohpic_ctx *c)
 int do_push(ohpic_ctx *c, double dt)
 {
     set_dt(c, dt);
-    cudaMemsetAsync(c->diag, 0, offsetof(DevDiag, kin), c->stream);   // crossings + outside
+    // crossings + outside (+ the kinetic sums when the push tracks them)
+    cudaMemsetAsync(c->diag, 0, c->with_energy ? offsetof(DevDiag, charge) : offsetof(DevDiag, kin), c->stream);
+    c->kin_valid = c->with_energy;
     launch_zero(c, c->rho, (int64_t)c->g.ncell * (c->cfg.precision == OHPIC_FP64 ? 8 : 4));
     if (c->push_timing) {
         // One event pair per push kernel, summed by ohpic_stats.
@@ -346,12 +348,12 @@ int ohpic_upload_particles_soa(ohpic_ctx *c, int s, const double *x, const doubl
             launch_f64_soa_from_stage(c, stage, m, c->seg[s] + a, (uint32_t)a, 0, 0);
         else
             launch_f64_to_f32(c, stage, m, c->seg[s] + a, (uint32_t)a, 0, 0);
-        // The stage is reused by the next chunk: order the copy after the conversion.
-        if (a + m < n) OHPIC_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        // The next chunk's copy into the stage is ordered after this conversion by the stream.
     }
     c->count[s] = n;
     c->sorted = false;
     c->rho_valid = false;
+    c->kin_valid = false;
     return check_device(c);
 }
 
@@ -371,11 +373,26 @@ int ohpic_upload_particles(ohpic_ctx *c, int s, const void *pbuf, int64_t n, int
             launch_f64_soa_from_stage(c, (const double *)c->stage, m, c->seg[s] + a, (uint32_t)a, 1, stride / 8);
         else
             launch_f64_to_f32(c, (const double *)c->stage, m, c->seg[s] + a, (uint32_t)a, 1, stride / 8);
-        if (a + m < n) OHPIC_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     }
     c->count[s] = n;
     c->sorted = false;
     c->rho_valid = false;
+    c->kin_valid = false;
+    return check_device(c);
+}
+
+int ohpic_init_particles(ohpic_ctx *c, uint64_t initstate, uint64_t initseq, uint64_t advance,
+                         const ohpic_species_init *species, int64_t *counts_out)
+{
+    if (!c || !species) return fail(c, OHPIC_ERR_INVALID, "init: null argument");
+    for (int s = 0; s < c->cfg.nspecies; ++s) {
+        const ohpic_species_init &p = species[s];
+        if (!(p.ppc >= 0.0) || !std::isfinite(p.ppc) || !(p.vth >= 0.0) || !std::isfinite(p.vth))
+            return fail(c, OHPIC_ERR_INVALID, "init: ppc and vth must be finite and >= 0");
+    }
+    cudaSetDevice(c->dev);
+    const int rc = init_particles(c, initstate, initseq, advance, species, counts_out);
+    if (rc != OHPIC_OK) return rc;
     return check_device(c);
 }
 
@@ -401,7 +418,6 @@ int ohpic_download_particles_soa(ohpic_ctx *c, int s, double *x, double *y, doub
         if (ids)
             OHPIC_CUDA_TRY(c, cudaMemcpyAsync(ids + a, c->ids[c->cur] + c->seg[s] + a, sizeof(uint32_t) * m,
                                               cudaMemcpyDeviceToHost, c->stream));
-        OHPIC_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     }
     return check_device(c);
 }
@@ -424,7 +440,6 @@ int ohpic_download_particles(ohpic_ctx *c, int s, void *pbuf, int64_t capacity, 
             OHPIC_CUDA_TRY(c, cudaMemcpy2DAsync((char *)pbuf + a * stride + 8 * k, (size_t)stride, stage + k * m,
                                                 sizeof(double), sizeof(double), (size_t)m, cudaMemcpyDeviceToHost,
                                                 c->stream));
-        OHPIC_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     }
     return check_device(c);
 }
@@ -485,6 +500,7 @@ int ohpic_move(ohpic_ctx *c, double dt)
     launch_tiled(c, MODE_MOVE, c->cfg.precision == OHPIC_FP64 ? 1 : 0);
     c->rho_valid = false;
     c->field_valid = false;
+    c->kin_valid = false;
     return OHPIC_OK;
 }
 
@@ -591,7 +607,7 @@ int ohpic_diagnostics(ohpic_ctx *c, ohpic_diag *d)
     cudaSetDevice(c->dev);
     if (!c->rho_valid) do_scatter(c);
     launch_field_energy(c);
-    launch_kinetic(c);
+    if (!c->kin_valid) launch_kinetic(c);
     OHPIC_CUDA_TRY(c, cudaMemcpyAsync(c->diag_host, c->diag, sizeof(DevDiag), cudaMemcpyDeviceToHost, c->stream));
     const int rc = check_device(c);
     if (rc != OHPIC_OK) return rc;
@@ -608,6 +624,14 @@ int ohpic_diagnostics(ohpic_ctx *c, ohpic_diag *d)
     d->step = c->steps;
     d->total_charge = h.charge;
     d->field_energy = h.field_energy;
+    return OHPIC_OK;
+}
+
+int ohpic_set_energy_tracking(ohpic_ctx *c, int enable)
+{
+    if (!c) return OHPIC_ERR_INVALID;
+    c->with_energy = enable != 0;
+    c->kin_valid = false;
     return OHPIC_OK;
 }
 

@@ -161,6 +161,7 @@ struct ohpic_ctx {
     int split;
     int halo;
     bool with_energy;
+    bool kin_valid;             // diag->kin holds the sums of the current velocities
 
     int64_t launches;
     int64_t push_launches;
@@ -194,6 +195,9 @@ void launch_f64_soa_from_stage(ohpic_ctx *c, const double *stage, int64_t n, int
                                int aos, int64_t stride_doubles);
 void launch_to_f64_stage(ohpic_ctx *c, double *stage, int64_t src, int64_t n);
 void launch_kinetic(ohpic_ctx *c);
+// Device-side initial conditions (init.cu).
+int init_particles(ohpic_ctx *c, uint64_t initstate, uint64_t initseq, uint64_t advance,
+                   const ohpic_species_init *spi, int64_t *counts);
 
 }  // namespace ohpic
 

@@ -268,6 +268,37 @@ def test_fp32_form_against_fp64_oracle(ohpic, oracle_mod, weights):
     ctx.close()
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_device_injector_matches_reference_streams(ohpic, oracle_mod, precision):
+    """ohpic_init_particles draws the reference injector's streams: counts and
+    positions identical, velocities within the device libm's last bits."""
+    P, O = ohpic, oracle_mod
+    n = (16, 8, 24)
+    species = [O.SpeciesInit(ppc=3, vth=1.0, qm=-1.0, wp=1.0),
+               O.SpeciesInit(ppc=2.5, vth=0.5, qm=-1.0, q=-0.1, drift=(0.0, 0.0, 5.0),
+                             lo=(0.35 * 16, 0.35 * 8, 0.0), hi=(0.65 * 16, 0.65 * 8, 24.0)),
+               O.SpeciesInit(ppc=4, vth=0.1, qm=0.01, wp=0.1)]
+    setup = O.Setup(n=n, dt=0.1, b0=(0, 0, 0.5), species=species, seed=(42, 77), rank_advance=12345)
+    o = O.Oracle(setup, threads=4)
+    o.init_particles()
+    caps = [o.count(s) + 64 for s in range(3)]
+    ctx = P.PicContext(_config(P, O, setup, caps, precision))
+    inits = [P.species_init(sp.ppc, sp.vth, sp.drift, *setup.range_of(sp)) for sp in species]
+    counts = ctx.init_particles(inits, seed=(42, 77), advance=12345)
+    assert counts == [o.count(s) for s in range(3)]
+    for s in range(3):
+        got, ref = ctx.download(s), o.get_particles(s)
+        for k in ("x", "y", "z"):
+            if precision == 0:
+                np.testing.assert_array_equal(got[k], ref[k])
+            else:
+                assert np.max(np.abs(got[k] - ref[k])) <= 2.0 ** -24 * 1.0001
+        for k in ("vx", "vy", "vz"):
+            tol = 1e-14 if precision == 0 else 2.0 ** -23
+            assert np.max(np.abs(got[k] - ref[k]) / (np.abs(ref[k]) + 1e-300)) <= tol
+    ctx.close()
+
+
 def test_sort_invariants(ohpic, oracle_mod):
     P, O = ohpic, oracle_mod
     setup = _two_species(O, (16, 16, 16), ppc=2)
