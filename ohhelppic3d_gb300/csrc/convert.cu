@@ -1,0 +1,241 @@
+// convert.cu -- conversions between the host FP64 particle records and the
+// device forms, kinetic-energy reduction, and the dispatch of the tiled kernels.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ohpic_internal.cuh"
+
+namespace ohpic {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ void flag_error(DevDiag *d, int code, int info)
+{
+    if (atomicCAS(&d->err_code, 0, code) == 0) d->err_info = info;
+}
+
+// ---------------------------------------------------------------------------
+// Conversions between the host's FP64 records and the device forms.
+// stage holds n particles either as 6 SoA arrays of n doubles (aos = 0) or as
+// AoS records of stride_doubles (aos = 1, x..vz at 0..5).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void read_stage(const double *s, int64_t i, int64_t n, int aos, int64_t stride,
+                                           double r[6])
+{
+    if (aos) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) r[k] = s[i * stride + k];
+    } else {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) r[k] = s[k * n + i];
+    }
+}
+
+__global__ void k_stage_to_f64(const double *stage, int64_t n, int aos, int64_t stride, PartF64 p, uint32_t *ids,
+                               int64_t dst, uint32_t id0)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double r[6];
+        read_stage(stage, i, n, aos, stride, r);
+        const int64_t o = dst + i;
+        p.x[o] = r[0]; p.y[o] = r[1]; p.z[o] = r[2];
+        p.vx[o] = r[3]; p.vy[o] = r[4]; p.vz[o] = r[5];
+        if (ids) ids[o] = id0 + (uint32_t)i;
+    }
+}
+
+// Absolute FP64 position -> (cell, FP32 offset).  The offset is rounded to
+// FP32; a value that rounds up to 1 moves to offset 0 of the next cell.
+__device__ __forceinline__ void split_pos(double x, int n, int &i, float &o, DevDiag *d)
+{
+    int c = (int)floor(x);
+    float f = (float)(x - (double)c);
+    if (f >= 1.f) { f = 0.f; ++c; }
+    if (c >= n) c -= n;
+    if (c < 0) c += n;
+    if ((unsigned)c >= (unsigned)n) {
+        flag_error(d, OHPIC_ERR_BOUNDS, 4);
+        c = 0;
+    }
+    i = c;
+    o = f;
+}
+
+__global__ void k_stage_to_f32(const double *stage, int64_t n, int aos, int64_t stride, PartF32 p, uint32_t *ids,
+                               int64_t dst, uint32_t id0, int nx, int ny, int nz, DevDiag *d)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double r[6];
+        read_stage(stage, i, n, aos, stride, r);
+        int ix, iy, iz;
+        float ox, oy, oz;
+        split_pos(r[0], nx, ix, ox, d);
+        split_pos(r[1], ny, iy, oy, d);
+        split_pos(r[2], nz, iz, oz, d);
+        const int64_t o = dst + i;
+        p.cell[o] = pack_cell(ix, iy, iz);
+        p.ox[o] = ox; p.oy[o] = oy; p.oz[o] = oz;
+        p.vx[o] = (float)r[3]; p.vy[o] = (float)r[4]; p.vz[o] = (float)r[5];
+        if (ids) ids[o] = id0 + (uint32_t)i;
+    }
+}
+
+// Device form -> 6 SoA arrays of n doubles (+ ids as the 7th block, reinterpreted).
+__global__ void k_f64_to_stage(PartF64 p, int64_t src, int64_t n, double *stage)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t o = src + i;
+        stage[i] = p.x[o]; stage[n + i] = p.y[o]; stage[2 * n + i] = p.z[o];
+        stage[3 * n + i] = p.vx[o]; stage[4 * n + i] = p.vy[o]; stage[5 * n + i] = p.vz[o];
+    }
+}
+
+__global__ void k_f32_to_stage(PartF32 p, int64_t src, int64_t n, double *stage)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t o = src + i;
+        const int32_t c = p.cell[o];
+        stage[i] = (double)cell_x(c) + (double)p.ox[o];
+        stage[n + i] = (double)cell_y(c) + (double)p.oy[o];
+        stage[2 * n + i] = (double)cell_z(c) + (double)p.oz[o];
+        stage[3 * n + i] = p.vx[o]; stage[4 * n + i] = p.vy[o]; stage[5 * n + i] = p.vz[o];
+    }
+}
+
+// Kinetic energy and momentum of every species (FP64 accumulation).
+template <bool F32>
+__global__ void k_kinetic(PartF64 p64, PartF32 p32, int64_t seg, int64_t n, double *out4)
+{
+    double ke = 0, mx = 0, my = 0, mz = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double vx, vy, vz;
+        if (F32) {
+            vx = p32.vx[seg + i]; vy = p32.vy[seg + i]; vz = p32.vz[seg + i];
+        } else {
+            vx = p64.vx[seg + i]; vy = p64.vy[seg + i]; vz = p64.vz[seg + i];
+        }
+        ke += vx * vx + vy * vy + vz * vz;
+        mx += vx; my += vy; mz += vz;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ke += __shfl_xor_sync(kFull, ke, o);
+        mx += __shfl_xor_sync(kFull, mx, o);
+        my += __shfl_xor_sync(kFull, my, o);
+        mz += __shfl_xor_sync(kFull, mz, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out4 + 0, ke);
+        atomicAdd(out4 + 1, mx);
+        atomicAdd(out4 + 2, my);
+        atomicAdd(out4 + 3, mz);
+    }
+}
+
+int grid_for(int64_t n, int threads)
+{
+    int64_t b = (n + threads - 1) / threads;
+    if (b > 152 * 32) b = 152 * 32;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+void launch_tiled(ohpic_ctx *c, int mode, int strict)
+{
+    TileArgs a;
+    a.g = c->g;
+    a.nspecies = c->cfg.nspecies;
+    a.weights = c->cfg.weights;
+    a.split = c->split;
+    a.with_energy = c->with_energy ? 1 : 0;
+    a.sorted = c->sorted ? 1 : 0;
+    a.chunk = 4096;
+    for (int s = 0; s < OHPIC_MAX_SPECIES; ++s) {
+        a.seg[s] = c->seg[s];
+        a.count[s] = c->count[s];
+        a.sc[s] = c->sc[s];
+    }
+    a.tile_begin = c->tile_begin;
+    a.epad = c->epad;
+    a.rho = c->rho;
+    a.wsum = c->wsum;
+    a.interp_out = c->interp_buf;
+    a.diag = c->diag;
+
+    const bool f64 = c->cfg.precision == OHPIC_FP64;
+    // particles per thread per iteration: 2 (FP64, double2 vectors) or 1 (FP32)
+    const int PPT = f64 ? 2 : 1;
+    int64_t blocks = 0;
+    if (a.sorted) {
+        blocks = (int64_t)a.nspecies * c->g.ntile * a.split;
+    } else {
+        for (int s = 0; s < a.nspecies; ++s) {
+            const int64_t groups = (c->count[s] + PPT - 1) / PPT;
+            blocks += (groups * PPT + a.chunk - 1) / a.chunk;
+        }
+    }
+    const int64_t s3 = (int64_t)c->g.sx * c->g.sy * c->g.sz;
+    const size_t es = f64 ? 8 : 4;
+    const bool gather = mode != MODE_DEPOSIT;
+    const bool dep = mode == MODE_PUSH || mode == MODE_DEPOSIT;
+    size_t smem = 0;
+    // E box: 4 reals per node; deposit box: one real per node (FP64) or the
+    // low and high 32-bit words of the fixed-point sums (FP32).
+    if (a.sorted) smem = (gather ? s3 * 4 * es : 0) + (dep ? s3 * 8 : 0);
+    if (f64)
+        launch_tiled_f64(c, a, mode, strict, blocks, smem);
+    else
+        launch_tiled_f32(c, a, mode, blocks, smem);
+}
+
+void launch_f64_soa_from_stage(ohpic_ctx *c, const double *stage, int64_t n, int64_t dst, uint32_t id0, int aos,
+                               int64_t stride_doubles)
+{
+    if (n <= 0) return;
+    k_stage_to_f64<<<grid_for(n, 256), 256, 0, c->stream>>>(stage, n, aos, stride_doubles, c->p64[c->cur],
+                                                             c->ids[c->cur], dst, id0);
+    ++c->launches;
+}
+
+void launch_f64_to_f32(ohpic_ctx *c, const double *stage, int64_t n, int64_t dst, uint32_t id0, int aos,
+                       int64_t stride_doubles)
+{
+    if (n <= 0) return;
+    k_stage_to_f32<<<grid_for(n, 256), 256, 0, c->stream>>>(stage, n, aos, stride_doubles, c->p32[c->cur],
+                                                             c->ids[c->cur], dst, id0, c->g.nx, c->g.ny,
+                                                             c->g.nz, c->diag);
+    ++c->launches;
+}
+
+void launch_to_f64_stage(ohpic_ctx *c, double *stage, int64_t src, int64_t n)
+{
+    if (n <= 0) return;
+    if (c->cfg.precision == OHPIC_FP64)
+        k_f64_to_stage<<<grid_for(n, 256), 256, 0, c->stream>>>(c->p64[c->cur], src, n, stage);
+    else
+        k_f32_to_stage<<<grid_for(n, 256), 256, 0, c->stream>>>(c->p32[c->cur], src, n, stage);
+    ++c->launches;
+}
+
+void launch_kinetic(ohpic_ctx *c)
+{
+    for (int s = 0; s < c->cfg.nspecies; ++s) {
+        double *out = &c->diag->kin[s][0];
+        cudaMemsetAsync(out, 0, 4 * sizeof(double), c->stream);
+        if (c->count[s] == 0) continue;
+        if (c->cfg.precision == OHPIC_FP64)
+            k_kinetic<false><<<grid_for(c->count[s], 256), 256, 0, c->stream>>>(c->p64[c->cur], c->p32[c->cur],
+                                                                                 c->seg[s], c->count[s], out);
+        else
+            k_kinetic<true><<<grid_for(c->count[s], 256), 256, 0, c->stream>>>(c->p64[c->cur], c->p32[c->cur],
+                                                                                c->seg[s], c->count[s], out);
+        ++c->launches;
+    }
+}
+
+}  // namespace ohpic

@@ -173,6 +173,22 @@ __global__ void k_field_sums(Geom g, const T *rho, const NodeT *epad, double *ch
     }
 }
 
+// FP32 form: rho = sum_s q_s * W_s * 2^-24 from the fixed-point weight sums,
+// evaluated in FP64 and rounded once to FP32.
+struct SpeciesCharges {
+    double q[OHPIC_MAX_SPECIES];
+    int nspecies;
+};
+
+__global__ void k_wsum_to_rho(const unsigned long long *w, int64_t ncell, SpeciesCharges sc, float *rho)
+{
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ncell; t += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int s = 0; s < sc.nspecies; ++s) acc += sc.q[s] * (double)w[s * ncell + t];
+        rho[t] = (float)(acc * kWeightUnit);
+    }
+}
+
 int blocks_for(int64_t n)
 {
     int64_t b = (n + 255) / 256;
@@ -181,6 +197,18 @@ int blocks_for(int64_t n)
 }
 
 }  // namespace
+
+// FP32 form: materialise rho from the weight sums left by the last deposit.
+void ensure_rho(ohpic_ctx *c)
+{
+    if (c->cfg.precision != OHPIC_FP32 || !c->rho_from_wsum) return;
+    SpeciesCharges sc;
+    sc.nspecies = c->cfg.nspecies;
+    for (int s = 0; s < OHPIC_MAX_SPECIES; ++s) sc.q[s] = s < sc.nspecies ? c->cfg.q[s] : 0.0;
+    k_wsum_to_rho<<<blocks_for(c->g.ncell), 256, 0, c->stream>>>(c->wsum, c->g.ncell, sc, (float *)c->rho);
+    ++c->launches;
+    c->rho_from_wsum = false;
+}
 
 int fields_setup(ohpic_ctx *c)
 {
@@ -217,6 +245,7 @@ void fields_teardown(ohpic_ctx *c)
 int solve_fields(ohpic_ctx *c)
 {
     const Geom &g = c->g;
+    ensure_rho(c);
     cufftResult r;
     if (c->cfg.precision == OHPIC_FP64) {
         r = cufftExecD2Z(c->plan_r2c, (cufftDoubleReal *)c->rho, (cufftDoubleComplex *)c->spec);
@@ -247,6 +276,7 @@ void launch_zero(ohpic_ctx *c, void *p, int64_t bytes) { cudaMemsetAsync(p, 0, (
 void launch_field_energy(ohpic_ctx *c)
 {
     const Geom &g = c->g;
+    ensure_rho(c);
     cudaMemsetAsync(&c->diag->charge, 0, 2 * sizeof(double), c->stream);
     if (c->cfg.precision == OHPIC_FP64)
         k_field_sums<double, dnode><<<blocks_for(g.ncell), 256, 0, c->stream>>>(
@@ -262,6 +292,7 @@ void field_to_double(ohpic_ctx *c, int which, double *dst)
 {
     const Geom &g = c->g;
     const bool f64 = c->cfg.precision == OHPIC_FP64;
+    if (which == OHPIC_RHO) ensure_rho(c);
     if (which == OHPIC_RHO || which == OHPIC_PHI) {
         const void *src = which == OHPIC_RHO ? c->rho : c->phi;
         if (f64)

@@ -101,9 +101,21 @@ bool species_ok(const ohpic_ctx *c, int s) { return c && s >= 0 && s < c->cfg.ns
 
 int ensure_fields(ohpic_ctx *c);
 
+// Clears the deposit target: rho (FP64 form) or the per-species fixed-point
+// weight sums (FP32 form, turned into rho by the next solve or download).
+void zero_deposit(ohpic_ctx *c)
+{
+    if (c->cfg.precision == OHPIC_FP64) {
+        launch_zero(c, c->rho, (int64_t)c->g.ncell * 8);
+    } else {
+        launch_zero(c, c->wsum, (int64_t)c->cfg.nspecies * c->g.ncell * 8);
+        c->rho_from_wsum = true;
+    }
+}
+
 int do_scatter(ohpic_ctx *c)
 {
-    launch_zero(c, c->rho, (int64_t)c->g.ncell * (c->cfg.precision == OHPIC_FP64 ? 8 : 4));
+    zero_deposit(c);
     launch_tiled(c, MODE_DEPOSIT, 0);
     c->rho_valid = true;
     return OHPIC_OK;
@@ -123,7 +135,7 @@ int do_push(ohpic_ctx *c, double dt)
     // crossings + outside (+ the kinetic sums when the push tracks them)
     cudaMemsetAsync(c->diag, 0, c->with_energy ? offsetof(DevDiag, charge) : offsetof(DevDiag, kin), c->stream);
     c->kin_valid = c->with_energy;
-    launch_zero(c, c->rho, (int64_t)c->g.ncell * (c->cfg.precision == OHPIC_FP64 ? 8 : 4));
+    zero_deposit(c);
     if (c->push_timing) {
         // One event pair per push kernel, summed by ohpic_stats.
         const size_t need = 2 * (size_t)(c->ev_used + 1);
@@ -195,7 +207,7 @@ int ohpic_destroy(ohpic_ctx *c)
         dfree(c->p32[b].vx); dfree(c->p32[b].vy); dfree(c->p32[b].vz);
         dfree(c->ids[b]);
     }
-    dfree(c->rho); dfree(c->phi); dfree(c->epad); dfree(c->spec); dfree(c->green);
+    dfree(c->rho); dfree(c->phi); dfree(c->epad); dfree(c->spec); dfree(c->green); dfree(c->wsum);
     dfree(c->cell_count); dfree(c->cell_start); dfree(c->scan_tmp); dfree(c->tile_begin);
     dfree(c->stage); dfree(c->interp_buf); dfree(c->diag);
     if (c->diag_host) cudaFreeHost(c->diag_host);
@@ -262,7 +274,7 @@ int ohpic_create(const ohpic_config *cfg, ohpic_ctx **out)
         // Staged E box (4 reals per node) plus the rho box must fit one CTA's shared memory.
         const int64_t s3 = (int64_t)g.sx * g.sy * g.sz;
         const int64_t es_ = k.precision == OHPIC_FP64 ? 8 : 4;
-        if (s3 * 5 * es_ > 200 * 1024) {
+        if (s3 * (4 * es_ + 8) > 200 * 1024) {
             ohpic_destroy(c);
             return OHPIC_ERR_INVALID;
         }
@@ -293,6 +305,7 @@ int ohpic_create(const ohpic_config *cfg, ohpic_ctx **out)
         if (rc == OHPIC_OK && k.track_ids) rc = dalloc(c, &c->ids[b], N);
     }
     if (rc == OHPIC_OK) rc = dalloc(c, (char **)&c->rho, g.ncell * es);
+    if (rc == OHPIC_OK && !f64) rc = dalloc(c, &c->wsum, (int64_t)k.nspecies * g.ncell);
     if (rc == OHPIC_OK) rc = dalloc(c, (char **)&c->phi, g.ncell * es);
     if (rc == OHPIC_OK) rc = dalloc(c, (char **)&c->epad, (int64_t)g.gx * g.gy * g.gz * 4 * es);
     if (rc == OHPIC_OK) rc = dalloc(c, (char **)&c->spec, g.nspec * 2 * es);
@@ -557,6 +570,7 @@ int ohpic_upload_field(ohpic_ctx *c, int which, const double *host)
     field_from_double(c, which, stage);
     if (which == OHPIC_RHO) {
         c->rho_valid = true;
+        c->rho_from_wsum = false;   // rho itself is now the charge density
         c->field_valid = false;
     } else if (which >= OHPIC_EX) {
         c->field_valid = true;

@@ -27,6 +27,9 @@ namespace ohpic {
 
 constexpr int kSegAlign = 64;       // particles; keeps every species segment 256-B aligned
 constexpr int kMaxHalo = 4;
+// FP32-form deposit: CIC weights in units of 2^-24 (the 8 weights of a particle sum to exactly 2^24).
+constexpr float kWeightScale = 16777216.0f;
+constexpr double kWeightUnit = 1.0 / 16777216.0;
 
 // Packed FP32-form cell index: 11 bits x, 11 bits y, 10 bits z.
 constexpr int kCellBitsX = 11, kCellBitsY = 11, kCellBitsZ = 10;
@@ -104,7 +107,8 @@ struct TileArgs {
     SpeciesConst sc[OHPIC_MAX_SPECIES];
     const int64_t *tile_begin;         // [nspecies][ntile+1], absolute array indices
     const void *epad;                  // padded E
-    void *rho;                         // n^3 (zeroed by the caller for deposit modes)
+    void *rho;                         // n^3 (zeroed by the caller for deposit modes); FP64 form
+    unsigned long long *wsum;          // FP32 form: [species][n^3] sums of CIC weights, 2^-24 fixed point
     double *interp_out;                // MODE_INTERP: 3 per particle slot (absolute index)
     DevDiag *diag;
     int chunk;                         // particles per CTA when unsorted
@@ -133,6 +137,11 @@ struct ohpic_ctx {
 
     // fields
     void *rho, *phi, *epad;
+    // FP32 form: the deposit accumulates per-species weight sums in 2^-24 fixed
+    // point (integer adds, so the result does not depend on the order of the
+    // atomics); the solve turns them into rho.
+    unsigned long long *wsum;
+    bool rho_from_wsum;
     void *spec;
     double *green;
     cufftHandle plan_r2c, plan_c2r;
@@ -175,8 +184,10 @@ struct ohpic_ctx {
 
 namespace ohpic {
 
-// Kernel launchers (particles.cu).
+// Kernel launchers: dispatch (convert.cu) and the two forms (push_f64.cu, push_f32.cu).
 void launch_tiled(ohpic_ctx *c, int mode, int strict);
+void launch_tiled_f64(ohpic_ctx *c, const TileArgs &a, int mode, int strict, int64_t blocks, size_t smem);
+void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks, size_t smem);
 // Fields (fields.cu).
 int fields_setup(ohpic_ctx *c);
 void fields_teardown(ohpic_ctx *c);
@@ -188,7 +199,7 @@ void field_from_double(ohpic_ctx *c, int which, const double *src);
 // Sort (sort.cu).
 int sort_particles(ohpic_ctx *c);
 int64_t scan_tmp_elems(int64_t n);
-// Conversions (particles.cu).
+// Conversions (convert.cu).
 void launch_f64_to_f32(ohpic_ctx *c, const double *stage6, int64_t n, int64_t dst, uint32_t id0,
                        int aos, int64_t stride_doubles);
 void launch_f64_soa_from_stage(ohpic_ctx *c, const double *stage, int64_t n, int64_t dst, uint32_t id0,
