@@ -213,6 +213,26 @@ int ohpic_synchronize(ohpic_ctx *ctx);
 /* The context's cudaStream_t, for callers that order their own work after it. */
 int ohpic_get_stream(ohpic_ctx *ctx, void **stream);
 
+/* Launch-shape tuning (no reference counterpart: the reference has no device
+ * kernels).  The autotuner (ohhelppic3d_gb300.autotune) times candidate values
+ * on the run's own particles and keeps the fastest per grid size. */
+enum {
+    OHPIC_DEPOSIT_RUNS = 0,       /* warp segmented reduction over runs of equal cells (shuffles) */
+    OHPIC_DEPOSIT_UNIFORM = 1,    /* whole-warp hardware reduce when all lanes share a cell, else runs */
+    OHPIC_DEPOSIT_MATCH = 2       /* match lanes by cell, hardware reduce per group */
+};
+typedef struct ohpic_tuning {
+    int32_t tile[3];            /* cells per tile edge; powers of two dividing n, <= 64 */
+    int32_t halo;               /* cells staged around a tile, 0..4 */
+    int32_t split;              /* CTAs per (species, tile), 1..64 */
+    int32_t deposit;            /* OHPIC_DEPOSIT_* (FP32 form) */
+    int32_t sort_every;         /* cell sort cadence in steps; 0 = only explicit sorts */
+} ohpic_tuning;
+int ohpic_get_tuning(ohpic_ctx *ctx, ohpic_tuning *out);
+/* Changing tile or halo re-lays out the staged E field: the next push solves
+ * again and the next step sorts again. */
+int ohpic_set_tuning(ohpic_ctx *ctx, const ohpic_tuning *tuning);
+
 /* Instrumentation: kernel launches issued by this context so far, and the
  * summed CUDA-event duration of the fused push kernel (enable first). */
 int ohpic_set_push_timing(ohpic_ctx *ctx, int enable);

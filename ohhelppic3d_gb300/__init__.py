@@ -70,6 +70,20 @@ def species_init(ppc, vth, drift=(0.0, 0.0, 0.0), lo=(0.0, 0.0, 0.0), hi=(1e30, 
     return s
 
 
+class Tuning(C.Structure):
+    _fields_ = [
+        ("tile", C.c_int32 * 3), ("halo", C.c_int32), ("split", C.c_int32),
+        ("deposit", C.c_int32), ("sort_every", C.c_int32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {"tile": tuple(self.tile), "halo": self.halo, "split": self.split,
+                "deposit": self.deposit, "sort_every": self.sort_every}
+
+
+DEPOSIT_RUNS, DEPOSIT_UNIFORM, DEPOSIT_MATCH = 0, 1, 2
+
+
 class OhpicError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"ohpic status {status}: {message}")
@@ -114,6 +128,8 @@ SIGNATURES = {
     "ohpic_set_push_timing": (C.c_int, [_P, C.c_int]),
     "ohpic_stats": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "ohpic_memory": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "ohpic_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "ohpic_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
 }
 
 
@@ -345,6 +361,21 @@ class PicContext:
         a, b, ms = C.c_int64(), C.c_int64(), C.c_double()
         self._check(lib().ohpic_stats(self.ptr, C.byref(a), C.byref(b), C.byref(ms)))
         return {"launches": a.value, "push_launches": b.value, "push_ms": ms.value}
+
+    def get_tuning(self) -> dict:
+        t = Tuning()
+        self._check(lib().ohpic_get_tuning(self.ptr, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, **kw):
+        cur = self.get_tuning()
+        cur.update(kw)
+        t = Tuning()
+        for d in range(3):
+            t.tile[d] = int(cur["tile"][d])
+        t.halo, t.split = int(cur["halo"]), int(cur["split"])
+        t.deposit, t.sort_every = int(cur["deposit"]), int(cur["sort_every"])
+        self._check(lib().ohpic_set_tuning(self.ptr, C.byref(t)))
 
     def memory(self) -> int:
         v = C.c_int64()

@@ -1,0 +1,159 @@
+"""Autotuner for the launch shape of the particle kernels.
+
+Picks, per grid size and plasma, the tile shape, the halo staged around a tile,
+the CTAs per (species, tile), the FP32 warp-deposit reduction and the cell-sort
+cadence.  It measures on a throwaway context filled by the device injector with
+the same particles per cell and physics as the run, so tuning never advances the
+caller's simulation.  The per-CTA work depends only on the tile and the plasma,
+not on the grid size, so large grids are tuned on a proxy grid (by default at
+most 128 x 128 x 64 cells) holding the same particles per cell; CTAs per tile
+only matter when the grid has few tiles, where the proxy is the grid itself.
+
+Search: coordinate descent from the library defaults -- deposit reduction, then
+tile shape, halo, split -- each candidate timed as the mean fused-push time over
+a few steps right after a sort; then the sort cadence K minimising
+(sort time + sum of push times over K steps) / K.
+"""
+from __future__ import annotations
+
+import json
+import os
+import time
+
+from . import DEPOSIT_MATCH, DEPOSIT_RUNS, DEPOSIT_UNIFORM, FP32, OhpicError, PicContext, make_config
+
+
+def _divisors(n: int) -> list:
+    return [t for t in (1, 2, 4, 8, 16, 32, 64) if n % t == 0]
+
+
+def _tiles(n) -> list:
+    """Candidate tile shapes: cubes and flat/tall boxes of power-of-two edges."""
+    shapes = [(4, 4, 4), (8, 8, 8), (8, 8, 4), (8, 4, 4), (16, 8, 8), (16, 8, 4), (8, 8, 16), (4, 4, 8),
+              (16, 16, 4), (2, 2, 2)]
+    out = []
+    for s in shapes:
+        if all(n[d] % s[d] == 0 for d in range(3)) and s not in out:
+            out.append(s)
+    return out or [tuple(max(_divisors(n[d])[-1:] or [1]) for d in range(3))]
+
+
+def proxy_grid(n, limit=(128, 128, 64)) -> tuple:
+    """The largest grid <= limit per axis that keeps every edge a multiple of 8 (when n is)."""
+    out = []
+    for d in range(3):
+        m = min(n[d], limit[d])
+        while n[d] % 8 == 0 and m % 8 != 0 and m > 8:
+            m -= 1
+        out.append(m)
+    return tuple(out)
+
+
+def _ctx(cfg_kw: dict, species: list, seed=(42, 4242)) -> PicContext:
+    ctx = PicContext(make_config(**cfg_kw))
+    ctx.init_particles(species, seed=seed)
+    return ctx
+
+
+def _push_ms(ctx: PicContext, dt: float, steps: int) -> float:
+    ctx.sort()
+    ctx.step(dt, 1)                      # first push after the sort (also re-solves)
+    ctx.set_push_timing(True)
+    ctx.step(dt, steps)
+    st = ctx.stats()
+    ctx.set_push_timing(False)
+    return st["push_ms"] / max(st["push_launches"], 1)
+
+
+def _sort_ms(ctx: PicContext) -> float:
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    ctx.sort()
+    ctx.synchronize()
+    return 1e3 * (time.perf_counter() - t0)
+
+
+def tune(n, dt, b0, qm, q, capacity_per_cell, species, precision=FP32, weights=0, proxy=True,
+         steps=3, max_cadence=40, log=None) -> dict:
+    """Returns the best tuning dict for a run on grid n.
+
+    species: list of SpeciesInit (device injector parameters) of the run;
+    capacity_per_cell: particles per cell to reserve per species (>= ppc)."""
+    grid = proxy_grid(n) if proxy else tuple(n)
+    ncell = grid[0] * grid[1] * grid[2]
+    caps = [int(c * ncell) + 1024 for c in capacity_per_cell]
+    cfg_kw = dict(n=grid, dt=dt, b0=b0, qm=qm, q=q, capacity=caps, precision=precision, weights=weights,
+                  sort_every=0)
+    ctx = _ctx(cfg_kw, species)
+    best = ctx.get_tuning()
+    trials = []
+
+    def measure(**kw):
+        try:
+            ctx.set_tuning(**kw)
+        except OhpicError:
+            return None
+        ms = _push_ms(ctx, dt, steps)
+        trials.append({**ctx.get_tuning(), "push_ms": ms})
+        if log:
+            log(f"tune {grid} {kw} -> {ms:.3f} ms")
+        return ms
+
+    def descend(key, values):
+        nonlocal best
+        base = dict(best)
+        scores = {}
+        for v in values:
+            s = measure(**{**base, key: v})
+            if s is not None:
+                scores[v] = s
+        if scores:
+            pick = min(scores, key=scores.get)
+            best = {**base, key: pick}
+            ctx.set_tuning(**best)
+
+    try:
+        if precision == FP32:
+            descend("deposit", [DEPOSIT_RUNS, DEPOSIT_UNIFORM, DEPOSIT_MATCH])
+        descend("tile", _tiles(grid))
+        descend("halo", [1, 2, 3])
+        if not proxy or grid == tuple(n):
+            descend("split", [1, 2, 4, 8])
+        # sort cadence: per-step push time grows as particles drift out of their tiles
+        sort_ms = _sort_ms(ctx)
+        ctx.set_push_timing(True)
+        pushes = []
+        for _ in range(max_cadence):
+            before = ctx.stats()["push_ms"]
+            ctx.step(dt, 1)
+            pushes.append(ctx.stats()["push_ms"] - before)
+        ctx.set_push_timing(False)
+        acc, cadence, cost = 0.0, 1, float("inf")
+        for k, p in enumerate(pushes, start=1):
+            acc += p
+            c = (sort_ms + acc) / k
+            if c < cost:
+                cost, cadence = c, k
+        best = {**best, "sort_every": cadence}
+    finally:
+        ctx.close()
+    best["grid_tuned_on"] = grid
+    best["trials"] = trials
+    best["sort_ms"] = sort_ms
+    best["push_ms_by_step_since_sort"] = pushes
+    return best
+
+
+def apply(ctx: PicContext, tuning: dict):
+    ctx.set_tuning(tile=tuning["tile"], halo=tuning["halo"], split=tuning.get("split", 1),
+                   deposit=tuning.get("deposit", DEPOSIT_RUNS), sort_every=tuning["sort_every"])
+
+
+def save(path: str, key: str, tuning: dict):
+    data = {}
+    if os.path.exists(path):
+        with open(path) as f:
+            data = json.load(f)
+    data[key] = {k: v for k, v in tuning.items() if k != "trials"}
+    with open(path, "w") as f:
+        json.dump(data, f, indent=1)

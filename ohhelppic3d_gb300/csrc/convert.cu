@@ -152,6 +152,9 @@ void launch_tiled(ohpic_ctx *c, int mode, int strict)
     a.nspecies = c->cfg.nspecies;
     a.weights = c->cfg.weights;
     a.split = c->split;
+    a.deposit = c->dep_strategy;
+    if (c->sorted && mode != MODE_DEPOSIT) ensure_emap(c);
+    a.use_tma = c->sorted && c->emap_ok ? 1 : 0;
     a.with_energy = c->with_energy ? 1 : 0;
     a.sorted = c->sorted ? 1 : 0;
     a.chunk = 4096;
@@ -186,7 +189,8 @@ void launch_tiled(ohpic_ctx *c, int mode, int strict)
     size_t smem = 0;
     // E box: 4 reals per node; deposit box: one real per node (FP64) or the
     // low and high 32-bit words of the fixed-point sums (FP32).
-    if (a.sorted) smem = (gather ? s3 * 4 * es : 0) + (dep ? s3 * 8 : 0);
+    // (+128: the kernels align the box start to 128 bytes for TMA)
+    if (a.sorted) smem = (gather ? s3 * 4 * es : 0) + (dep ? s3 * 8 : 0) + 128;
     if (f64)
         launch_tiled_f64(c, a, mode, strict, blocks, smem);
     else

@@ -36,6 +36,31 @@ int default_tile(int n)
     return 1;
 }
 
+// Grid geometry for a tile shape and halo; false when a tile edge is not a
+// divisor of the grid or the staged box does not fit one CTA's shared memory.
+bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g)
+{
+    const int n[3] = {k.nx, k.ny, k.nz};
+    for (int d = 0; d < 3; ++d)
+        if (tile[d] < 1 || tile[d] > 64 || n[d] % tile[d] != 0) return false;
+    if (halo < 0 || halo > kMaxHalo) return false;
+    g.nx = k.nx; g.ny = k.ny; g.nz = k.nz;
+    g.tx = tile[0]; g.ty = tile[1]; g.tz = tile[2];
+    g.ntx = g.nx / g.tx; g.nty = g.ny / g.ty; g.ntz = g.nz / g.tz;
+    g.halo = halo;
+    g.sx = g.tx + 2 * halo + 1; g.sy = g.ty + 2 * halo + 1; g.sz = g.tz + 2 * halo + 1;
+    g.gx = g.nx + 2 * halo + 1; g.gy = g.ny + 2 * halo + 1; g.gz = g.nz + 2 * halo + 1;
+    g.ncell = (int64_t)g.nx * g.ny * g.nz;
+    g.ntile = (int64_t)g.ntx * g.nty * g.ntz;
+    g.tile_cells = g.tx * g.ty * g.tz;
+    g.nxh = g.nx / 2 + 1;
+    g.nspec = (int64_t)g.nxh * g.ny * g.nz;
+    // Staged E box (4 reals per node) plus the deposit box (8 bytes per node).
+    const int64_t s3 = (int64_t)g.sx * g.sy * g.sz;
+    const int64_t es = k.precision == OHPIC_FP64 ? 8 : 4;
+    return s3 * (4 * es + 8) <= 200 * 1024;
+}
+
 // Boris constants of one species for a time step (particle_mover_boris.f90:37-43),
 // evaluated in FP64 in the reference's operation order (host code is built
 // with -ffp-contract=off).
@@ -258,26 +283,11 @@ int ohpic_create(const ohpic_config *cfg, ohpic_ctx **out)
     c->split = 1;
     c->with_energy = false;
     c->sc_dt = NAN;
+    c->dep_strategy = OHPIC_DEPOSIT_RUNS;
     Geom &g = c->g;
-    g.nx = k.nx; g.ny = k.ny; g.nz = k.nz;
-    g.tx = tile[0]; g.ty = tile[1]; g.tz = tile[2];
-    g.ntx = g.nx / g.tx; g.nty = g.ny / g.ty; g.ntz = g.nz / g.tz;
-    g.halo = c->halo;
-    g.sx = g.tx + 2 * g.halo + 1; g.sy = g.ty + 2 * g.halo + 1; g.sz = g.tz + 2 * g.halo + 1;
-    g.gx = g.nx + 2 * g.halo + 1; g.gy = g.ny + 2 * g.halo + 1; g.gz = g.nz + 2 * g.halo + 1;
-    g.ncell = (int64_t)g.nx * g.ny * g.nz;
-    g.ntile = (int64_t)g.ntx * g.nty * g.ntz;
-    g.tile_cells = g.tx * g.ty * g.tz;
-    g.nxh = g.nx / 2 + 1;
-    g.nspec = (int64_t)g.nxh * g.ny * g.nz;
-    {
-        // Staged E box (4 reals per node) plus the rho box must fit one CTA's shared memory.
-        const int64_t s3 = (int64_t)g.sx * g.sy * g.sz;
-        const int64_t es_ = k.precision == OHPIC_FP64 ? 8 : 4;
-        if (s3 * (4 * es_ + 8) > 200 * 1024) {
-            ohpic_destroy(c);
-            return OHPIC_ERR_INVALID;
-        }
+    if (!make_geom(k, tile, c->halo, g)) {
+        ohpic_destroy(c);
+        return OHPIC_ERR_INVALID;
     }
 
     int64_t off = 0;
@@ -714,6 +724,60 @@ int ohpic_memory(ohpic_ctx *c, int64_t *bytes)
 {
     if (!c || !bytes) return OHPIC_ERR_INVALID;
     *bytes = c->device_bytes;
+    return OHPIC_OK;
+}
+
+int ohpic_get_tuning(ohpic_ctx *c, ohpic_tuning *t)
+{
+    if (!c || !t) return OHPIC_ERR_INVALID;
+    t->tile[0] = c->g.tx;
+    t->tile[1] = c->g.ty;
+    t->tile[2] = c->g.tz;
+    t->halo = c->g.halo;
+    t->split = c->split;
+    t->deposit = c->dep_strategy;
+    t->sort_every = c->cfg.sort_every;
+    return OHPIC_OK;
+}
+
+int ohpic_set_tuning(ohpic_ctx *c, const ohpic_tuning *t)
+{
+    if (!c || !t) return OHPIC_ERR_INVALID;
+    if (t->split < 1 || t->split > 64 || t->deposit < OHPIC_DEPOSIT_RUNS || t->deposit > OHPIC_DEPOSIT_MATCH ||
+        t->sort_every < 0)
+        return fail(c, OHPIC_ERR_INVALID, "tuning: split 1..64, deposit 0..2, sort_every >= 0");
+    Geom g2;
+    if (!make_geom(c->cfg, t->tile, t->halo, g2))
+        return fail(c, OHPIC_ERR_INVALID, "tuning: tile edges must divide the grid (<= 64) and the staged box fit");
+    cudaSetDevice(c->dev);
+    const bool relayout = g2.tx != c->g.tx || g2.ty != c->g.ty || g2.tz != c->g.tz || g2.halo != c->g.halo;
+    if (relayout) {
+        OHPIC_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        const int64_t es = c->cfg.precision == OHPIC_FP64 ? 8 : 4;
+        if (g2.halo != c->g.halo) {
+            dfree(c->epad);
+            c->device_bytes -= (int64_t)c->g.gx * c->g.gy * c->g.gz * 4 * es;
+            int rc = dalloc(c, (char **)&c->epad, (int64_t)g2.gx * g2.gy * g2.gz * 4 * es);
+            if (rc != OHPIC_OK) return rc;
+            cudaMemsetAsync(c->epad, 0, (size_t)g2.gx * g2.gy * g2.gz * 4 * es, c->stream);
+        }
+        if (g2.ntile != c->g.ntile) {
+            dfree(c->tile_begin);
+            c->device_bytes -= (int64_t)c->cfg.nspecies * (c->g.ntile + 1) * 8;
+            int rc = dalloc(c, &c->tile_begin, (int64_t)c->cfg.nspecies * (g2.ntile + 1));
+            if (rc != OHPIC_OK) return rc;
+        }
+        c->g = g2;
+        c->halo = g2.halo;
+        c->cfg.tile[0] = g2.tx;
+        c->cfg.tile[1] = g2.ty;
+        c->cfg.tile[2] = g2.tz;
+        c->sorted = false;
+        c->field_valid = false;
+    }
+    c->split = t->split;
+    c->dep_strategy = t->deposit;
+    c->cfg.sort_every = t->sort_every;
     return OHPIC_OK;
 }
 

@@ -14,6 +14,7 @@
 //   spectrum             : nz*ny*(nx/2+1) complex (cuFFT R2C layout); green: same, FP64
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <stdint.h>
@@ -100,6 +101,8 @@ struct TileArgs {
     int nspecies;
     int weights;                       // OHPIC_WEIGHTS_*
     int split;                         // CTAs per (species, tile)
+    int deposit;                       // OHPIC_DEPOSIT_* (FP32 form)
+    int use_tma;                       // stage the E box with cp.async.bulk.tensor
     int with_energy;                   // accumulate kinetic energy / momentum
     int sorted;                        // tile_begin valid
     int64_t seg[OHPIC_MAX_SPECIES];
@@ -142,6 +145,11 @@ struct ohpic_ctx {
     // atomics); the solve turns them into rho.
     unsigned long long *wsum;
     bool rho_from_wsum;
+    // TMA description of epad for staging a tile's E box (tma_map.cu).
+    CUtensorMap emap;   // carries its own alignment
+    bool emap_ok;
+    void *emap_for;
+    int emap_key[4];
     void *spec;
     double *green;
     cufftHandle plan_r2c, plan_c2r;
@@ -169,6 +177,7 @@ struct ohpic_ctx {
     int64_t steps;
     int split;
     int halo;
+    int dep_strategy;           // OHPIC_DEPOSIT_* for the FP32 warp deposit
     bool with_energy;
     bool kin_valid;             // diag->kin holds the sums of the current velocities
 
@@ -188,6 +197,7 @@ namespace ohpic {
 void launch_tiled(ohpic_ctx *c, int mode, int strict);
 void launch_tiled_f64(ohpic_ctx *c, const TileArgs &a, int mode, int strict, int64_t blocks, size_t smem);
 void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks, size_t smem);
+void ensure_emap(ohpic_ctx *c);
 // Fields (fields.cu).
 int fields_setup(ohpic_ctx *c);
 void fields_teardown(ohpic_ctx *c);

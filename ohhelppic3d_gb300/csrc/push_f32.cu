@@ -26,15 +26,15 @@
 // per-species 64-bit global sums.  All of it is integer addition, so the deposit
 // does not depend on the order in which atomics land.
 #include "tile_common.cuh"
+#include "tma.cuh"
 
 namespace ohpic {
 namespace {
 
-// Sums u over each run of equal keys held by adjacent lanes; the run's first
-// lane adds the totals to the shared box when its key is a box index (>= 0).
-// All 32 lanes must call this.
-__device__ __forceinline__ void warp_run_deposit(int key, unsigned u[8], unsigned *lo, unsigned *hi, int sx,
-                                                 int sxy)
+// Segmented sum of u over runs of equal keys held by adjacent lanes (at most 5
+// shuffle steps, stopping early when the runs are short); returns true in the
+// run's first lane, which then holds the run total.
+__device__ __forceinline__ bool run_sum(int key, unsigned u[8])
 {
     const int lane = (int)(threadIdx.x & 31u);
     const int prev = __shfl_up_sync(kFull, key, 1);
@@ -52,15 +52,54 @@ __device__ __forceinline__ void warp_run_deposit(int key, unsigned u[8], unsigne
             if (take) u[v] += t;
         }
     }
-    if (head && key >= 0) {
-        const int off[8] = {0, 1, sx, sx + 1, sxy, sxy + 1, sxy + sx, sxy + sx + 1};
-        unsigned old[8];
+    return head;
+}
+
+// Deposit box: a node's weight sum (units of 2^-24) is the 64-bit value
+// hi:lo kept in two 32-bit words; an add goes to lo with a native 32-bit
+// shared atomic and a carry out of lo increments hi.
+__device__ __forceinline__ void box_add8(unsigned *hi, unsigned *lo, int key, int sx, int sxy, const unsigned u[8])
+{
+    const int off[8] = {0, 1, sx, sx + 1, sxy, sxy + 1, sxy + sx, sxy + sx + 1};
+    unsigned old[8];
 #pragma unroll
-        for (int v = 0; v < 8; ++v) old[v] = atomicAdd(lo + key + off[v], u[v]);
+    for (int v = 0; v < 8; ++v) old[v] = atomicAdd(lo + key + off[v], u[v]);
 #pragma unroll
-        for (int v = 0; v < 8; ++v)
-            if (old[v] + u[v] < old[v]) atomicAdd(hi + key + off[v], 1u);   // carry out of the low word
+    for (int v = 0; v < 8; ++v)
+        if (old[v] + u[v] < old[v]) atomicAdd(hi + key + off[v], 1u);
+}
+
+// Adds u (weights, key = box index of the cell or < 0) to the shared box after
+// combining the lanes that share a key.  DEP picks the combination
+// (OHPIC_DEPOSIT_*): runs of adjacent lanes by shuffles; one hardware warp
+// reduce when every lane holds the same key, else runs; or __match_any_sync
+// groups reduced with __reduce_add_sync.  All 32 lanes must call this.
+template <int DEP>
+__device__ __forceinline__ void warp_run_deposit(int key, unsigned u[8], unsigned *lo, unsigned *hi, int sx,
+                                                 int sxy)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    bool head;
+    if (DEP == OHPIC_DEPOSIT_MATCH) {
+        const unsigned peers = __match_any_sync(kFull, key);
+        head = (peers & ((1u << lane) - 1u)) == 0u;
+        if (peers != (1u << lane)) {
+#pragma unroll
+            for (int v = 0; v < 8; ++v) u[v] = __reduce_add_sync(peers, u[v]);
+        }
+    } else if (DEP == OHPIC_DEPOSIT_UNIFORM) {
+        const int k0 = __shfl_sync(kFull, key, 0);
+        if (__all_sync(kFull, key == k0)) {
+#pragma unroll
+            for (int v = 0; v < 8; ++v) u[v] = __reduce_add_sync(kFull, u[v]);
+            head = lane == 0;
+        } else {
+            head = run_sum(key, u);
+        }
+    } else {
+        head = run_sum(key, u);
     }
+    if (head && key >= 0) box_add8(hi, lo, key, sx, sxy, u);
 }
 
 // CIC weights of one particle in units of 2^-24, summing to exactly 2^24: the
@@ -73,11 +112,12 @@ __device__ __forceinline__ void fixed_weights(int conv, float ox, float oy, floa
     cic<float>(conv, oy, wy0, wy1);
     cic<float>(conv, oz, wz0, wz1);
     const float a00 = wx0 * wy0, a10 = wx1 * wy0, a01 = wx0 * wy1, a11 = wx1 * wy1;
-    const float f[8] = {a00 * wz0, a10 * wz0, a01 * wz0, a11 * wz0, a00 * wz1, a10 * wz1, a01 * wz1, a11 * wz1};
+    const float sz0 = wz0 * kWeightScale, sz1 = wz1 * kWeightScale;   // exact: power-of-two scale
+    const float f[8] = {a00 * sz0, a10 * sz0, a01 * sz0, a11 * sz0, a00 * sz1, a10 * sz1, a01 * sz1, a11 * sz1};
     unsigned sum = 0;
 #pragma unroll
     for (int v = 0; v < 8; ++v) {
-        u[v] = __float2uint_rn(f[v] * kWeightScale);
+        u[v] = __float2uint_rn(f[v]);
         sum += u[v];
     }
     const int big = (wx1 > wx0 ? 1 : 0) + (wy1 > wy0 ? 2 : 0) + (wz1 > wz0 ? 4 : 0);
@@ -108,17 +148,21 @@ __device__ __forceinline__ void deposit_global_fixed(const Geom &g, unsigned lon
 __device__ __forceinline__ void stage_f32(const TileArgs &a, const Item &it, float4 *sE, unsigned *lo, unsigned *hi,
                                           bool need_e, bool need_w)
 {
+    // One box row (fixed y, z) per warp iteration, lanes along x.
     const Geom &g = a.g;
-    const int s3 = g.sx * g.sy * g.sz;
     const float4 *E = (const float4 *)a.epad;
-    for (int i = threadIdx.x; i < s3; i += blockDim.x) {
-        if (need_e) {
-            const int ax = i % g.sx, by = (i / g.sx) % g.sy, cz = i / (g.sx * g.sy);
-            sE[i] = __ldg(E + ((int64_t)(it.z0 + cz) * g.gy + (it.y0 + by)) * g.gx + (it.x0 + ax));
-        }
-        if (need_w) {
-            lo[i] = 0u;
-            hi[i] = 0u;
+    const int rows = g.sy * g.sz, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int r = threadIdx.x >> 5; r < rows; r += nw) {
+        const int cz = r / g.sy, by = r - cz * g.sy;
+        // padded index of node x0 - halo + ax is x0 + ax
+        const float4 *src = E + ((int64_t)(it.z0 + cz) * g.gy + (it.y0 + by)) * g.gx + it.x0;
+        const int base = r * g.sx;
+        for (int ax = lane; ax < g.sx; ax += 32) {
+            if (need_e) sE[base + ax] = __ldg(src + ax);
+            if (need_w) {
+                lo[base + ax] = 0u;
+                hi[base + ax] = 0u;
+            }
         }
     }
 }
@@ -126,16 +170,21 @@ __device__ __forceinline__ void stage_f32(const TileArgs &a, const Item &it, flo
 __device__ __forceinline__ void flush_f32(const TileArgs &a, const Item &it, const unsigned *lo, const unsigned *hi)
 {
     const Geom &g = a.g;
-    const int s3 = g.sx * g.sy * g.sz;
     unsigned long long *w = a.wsum + (int64_t)it.sp * g.ncell;
-    for (int i = threadIdx.x; i < s3; i += blockDim.x) {
-        const unsigned long long v = ((unsigned long long)hi[i] << 32) | lo[i];
-        if (v) {
-            const int ax = i % g.sx, by = (i / g.sx) % g.sy, cz = i / (g.sx * g.sy);
-            const int x = wrapi(it.x0 - g.halo + ax, g.nx);
-            const int y = wrapi(it.y0 - g.halo + by, g.ny);
-            const int z = wrapi(it.z0 - g.halo + cz, g.nz);
-            atomicAdd(w + x + (int64_t)g.nx * (y + (int64_t)g.ny * z), v);
+    const int rows = g.sy * g.sz, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int r = threadIdx.x >> 5; r < rows; r += nw) {
+        const int cz = r / g.sy, by = r - cz * g.sy;
+        const int y = wrapi(it.y0 - g.halo + by, g.ny);
+        const int z = wrapi(it.z0 - g.halo + cz, g.nz);
+        unsigned long long *row = w + (int64_t)g.nx * (y + (int64_t)g.ny * z);
+        const int base = r * g.sx;
+        for (int ax = lane; ax < g.sx; ax += 32) {
+            const unsigned long long v = ((unsigned long long)hi[base + ax] << 32) | lo[base + ax];
+            if (v) {
+                int x = it.x0 - g.halo + ax;
+                if ((unsigned)x >= (unsigned)g.nx) x = wrapi(x, g.nx);
+                atomicAdd(row + x, v);
+            }
         }
     }
 }
@@ -161,8 +210,8 @@ __device__ __forceinline__ void load_p(const PartF32 &p, int64_t i, P32 &r)
     }
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(256, 3) tiled_f32(TileArgs a, PartF32 p)
+template <int MODE, int DEP>
+__global__ void __launch_bounds__(256, 3) tiled_f32(TileArgs a, PartF32 p, const __grid_constant__ CUtensorMap emap)
 {
     constexpr bool kGather = MODE != MODE_DEPOSIT;
     constexpr bool kMove = MODE == MODE_PUSH || MODE == MODE_MOVE;
@@ -172,14 +221,29 @@ __global__ void __launch_bounds__(256, 3) tiled_f32(TileArgs a, PartF32 p)
     if (!get_item<1>(a, it)) return;
     const Geom &g = a.g;
     const Box box = make_box(g, it);
-    extern __shared__ __align__(16) unsigned char smem[];
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t ebar;
+    // box start aligned to 128 bytes (the launch reserves the slack)
+    unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
     const int s3 = g.sx * g.sy * g.sz;
     float4 *sE = (float4 *)smem;
     unsigned *slo = (unsigned *)(smem + (kGather ? (size_t)s3 * sizeof(float4) : 0));
     unsigned *shi = slo + s3;
+    // The E box arrives by one TMA copy while the threads clear the deposit box.
+    const bool tma = box.on && kGather && a.use_tma;
+    if (tma && threadIdx.x == 0) {
+        mbar_init(&ebar, 1);
+        mbar_expect_tx(&ebar, (uint32_t)(s3 * sizeof(float4)));
+        tma_load_3d(sE, &emap, 4 * it.x0, it.y0, it.z0, &ebar);
+    }
     if (box.on) {
-        stage_f32(a, it, sE, slo, shi, kGather, kDeposit);
+        stage_f32(a, it, sE, slo, shi, kGather && !tma, kDeposit);
         __syncthreads();
+    }
+    bool e_ok = box.on;
+    if (tma && !mbar_wait(&ebar, 0, kTmaWaitPolls)) {
+        flag_error(a.diag, OHPIC_ERR_TIMEOUT, 5);
+        e_ok = false;   // gather from global memory instead
     }
 
     const int sp = it.sp;
@@ -220,7 +284,7 @@ __global__ void __launch_bounds__(256, 3) tiled_f32(TileArgs a, PartF32 p)
                 const float ww[8] = {a00 * wz0, a10 * wz0, a01 * wz0, a11 * wz0,
                                      a00 * wz1, a10 * wz1, a01 * wz1, a11 * wz1};
                 float4 nd[8];
-                load_nodes<float4>(a, box, key, ix, iy, iz, sE, nd);
+                load_nodes<float4>(a, box, e_ok ? key : -1, ix, iy, iz, sE, nd);
                 float ex = 0.f, ey = 0.f, ez = 0.f;
 #pragma unroll
                 for (int n = 0; n < 8; ++n) {
@@ -280,7 +344,7 @@ __global__ void __launch_bounds__(256, 3) tiled_f32(TileArgs a, PartF32 p)
                 p.vx[i] = cur.vx; p.vy[i] = cur.vy; p.vz[i] = cur.vz;
             }
         }
-        if (kDeposit) warp_run_deposit(dkey, w, slo, shi, box.sx, box.sxy);
+        if (kDeposit) warp_run_deposit<DEP>(dkey, w, slo, shi, box.sx, box.sxy);
         i = inext;
         valid = vnext;
         cur = nxt;
@@ -295,12 +359,12 @@ __global__ void __launch_bounds__(256, 3) tiled_f32(TileArgs a, PartF32 p)
 }  // namespace
 
 template <typename P>
-static void launch_k(ohpic_ctx *c, void (*kernel)(TileArgs, P), const TileArgs &a, int64_t blocks, size_t smem,
-                     const P &parts)
+static void launch_k(ohpic_ctx *c, void (*kernel)(TileArgs, P, const CUtensorMap), const TileArgs &a,
+                     int64_t blocks, size_t smem, const P &parts)
 {
     if (blocks <= 0) return;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kernel<<<(unsigned)blocks, 256, smem, c->stream>>>(a, parts);
+    kernel<<<(unsigned)blocks, 256, smem, c->stream>>>(a, parts, c->emap);
     ++c->launches;
 }
 
@@ -308,10 +372,22 @@ void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks,
 {
     const PartF32 &pp = c->p32[c->cur];
     switch (mode) {
-    case MODE_PUSH: launch_k(c, tiled_f32<MODE_PUSH>, a, blocks, smem, pp); break;
-    case MODE_MOVE: launch_k(c, tiled_f32<MODE_MOVE>, a, blocks, smem, pp); break;
-    case MODE_DEPOSIT: launch_k(c, tiled_f32<MODE_DEPOSIT>, a, blocks, smem, pp); break;
-    case MODE_INTERP: launch_k(c, tiled_f32<MODE_INTERP>, a, blocks, smem, pp); break;
+    case MODE_PUSH:
+        if (a.deposit == OHPIC_DEPOSIT_MATCH)
+            launch_k(c, tiled_f32<MODE_PUSH, OHPIC_DEPOSIT_MATCH>, a, blocks, smem, pp);
+        else if (a.deposit == OHPIC_DEPOSIT_UNIFORM)
+            launch_k(c, tiled_f32<MODE_PUSH, OHPIC_DEPOSIT_UNIFORM>, a, blocks, smem, pp);
+        else launch_k(c, tiled_f32<MODE_PUSH, OHPIC_DEPOSIT_RUNS>, a, blocks, smem, pp);
+        break;
+    case MODE_DEPOSIT:
+        if (a.deposit == OHPIC_DEPOSIT_MATCH)
+            launch_k(c, tiled_f32<MODE_DEPOSIT, OHPIC_DEPOSIT_MATCH>, a, blocks, smem, pp);
+        else if (a.deposit == OHPIC_DEPOSIT_UNIFORM)
+            launch_k(c, tiled_f32<MODE_DEPOSIT, OHPIC_DEPOSIT_UNIFORM>, a, blocks, smem, pp);
+        else launch_k(c, tiled_f32<MODE_DEPOSIT, OHPIC_DEPOSIT_RUNS>, a, blocks, smem, pp);
+        break;
+    case MODE_MOVE: launch_k(c, tiled_f32<MODE_MOVE, OHPIC_DEPOSIT_RUNS>, a, blocks, smem, pp); break;
+    case MODE_INTERP: launch_k(c, tiled_f32<MODE_INTERP, OHPIC_DEPOSIT_RUNS>, a, blocks, smem, pp); break;
     }
 }
 
