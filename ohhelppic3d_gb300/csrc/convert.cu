@@ -171,8 +171,8 @@ void launch_tiled(ohpic_ctx *c, int mode, int strict)
     a.diag = c->diag;
 
     const bool f64 = c->cfg.precision == OHPIC_FP64;
-    // particles per thread per iteration: 2 (FP64, double2 vectors) or 1 (FP32)
-    const int PPT = f64 ? 2 : 1;
+    // particles per thread per iteration: 2 in both forms (double2 / float2 vectors)
+    const int PPT = 2;
     int64_t blocks = 0;
     if (a.sorted) {
         blocks = (int64_t)a.nspecies * c->g.ntile * a.split;

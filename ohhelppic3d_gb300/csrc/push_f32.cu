@@ -9,12 +9,12 @@
 // Particle state: int32 packed cell (ix | iy<<11 | iz<<22), FP32 offsets in
 // [0, 1) and FP32 velocities, 28 bytes per particle in 7 SoA arrays.
 //
-// Mapping.  Lane l of a warp handles particle base + l, so the 32 lanes hold 32
-// consecutive particles of the cell-sorted order: their cells are mostly the
+// Mapping.  Lane l of a warp handles particles base + 2l and base + 2l + 1, so
+// the 32 lanes hold 64 consecutive particles of the cell-sorted order: their cells are mostly the
 // same one or two, the 8 node loads of the gather are shared-memory broadcasts,
 // and their deposits form runs of equal cells across adjacent lanes.  Loads and
-// stores are 4-byte coalesced accesses; the next batch's 7 values are loaded
-// before the current batch is computed.
+// stores are 8-byte vector accesses coalesced across the warp; the next pair's
+// 7 vectors are loaded before the current pair is computed.
 //
 // Deposit in fixed point.  Each particle's 8 CIC weights are rounded to units of
 // 2^-24 with the largest one adjusted so they sum to exactly 2^24 (charge is
@@ -194,31 +194,150 @@ struct P32 {
     float ox, oy, oz, vx, vy, vz;
 };
 
+// Particles 2g and 2g+1: one 8-byte vector per array.
 template <bool kGather>
-__device__ __forceinline__ void load_p(const PartF32 &p, int64_t i, P32 &r)
+__device__ __forceinline__ void load_pair(const PartF32 &p, int64_t g, P32 r[2])
 {
-    r.cell = p.cell[i];
-    r.ox = p.ox[i];
-    r.oy = p.oy[i];
-    r.oz = p.oz[i];
+    const int2 c = *(const int2 *)(p.cell + 2 * g);
+    const float2 x = *(const float2 *)(p.ox + 2 * g);
+    const float2 y = *(const float2 *)(p.oy + 2 * g);
+    const float2 z = *(const float2 *)(p.oz + 2 * g);
+    r[0].cell = c.x; r[1].cell = c.y;
+    r[0].ox = x.x; r[1].ox = x.y;
+    r[0].oy = y.x; r[1].oy = y.y;
+    r[0].oz = z.x; r[1].oz = z.y;
     if (kGather) {
-        r.vx = p.vx[i];
-        r.vy = p.vy[i];
-        r.vz = p.vz[i];
+        const float2 u = *(const float2 *)(p.vx + 2 * g);
+        const float2 v = *(const float2 *)(p.vy + 2 * g);
+        const float2 w = *(const float2 *)(p.vz + 2 * g);
+        r[0].vx = u.x; r[1].vx = u.y;
+        r[0].vy = v.x; r[1].vy = v.y;
+        r[0].vz = w.x; r[1].vz = w.y;
     } else {
-        r.vx = r.vy = r.vz = 0.f;
+        r[0].vx = r[0].vy = r[0].vz = r[1].vx = r[1].vy = r[1].vz = 0.f;
     }
 }
 
+__device__ __forceinline__ void store_pair(const PartF32 &p, int64_t g, const P32 r[2])
+{
+    *(int2 *)(p.cell + 2 * g) = make_int2(r[0].cell, r[1].cell);
+    *(float2 *)(p.ox + 2 * g) = make_float2(r[0].ox, r[1].ox);
+    *(float2 *)(p.oy + 2 * g) = make_float2(r[0].oy, r[1].oy);
+    *(float2 *)(p.oz + 2 * g) = make_float2(r[0].oz, r[1].oz);
+    *(float2 *)(p.vx + 2 * g) = make_float2(r[0].vx, r[1].vx);
+    *(float2 *)(p.vy + 2 * g) = make_float2(r[0].vy, r[1].vy);
+    *(float2 *)(p.vz + 2 * g) = make_float2(r[0].vz, r[1].vz);
+}
+
+// FP32 Boris constants of one species.
+struct Push32 {
+    float hq;            // qm*dt/2: E -> half kick of the velocity
+    float dt;
+    float t0, t1, t2, s0, s1, s2;
+};
+
+// Per-thread diagnostics.
+struct Tally {
+    unsigned cx = 0, cy = 0, cz = 0, out = 0;
+    float ke = 0.f, px = 0.f, py = 0.f, pz = 0.f;
+};
+
+// One particle: gather (MODE != DEPOSIT), Boris + offset update + periodic cell
+// wrap (PUSH/MOVE), interp output (INTERP) and the fixed-point CIC weights of
+// the (new) position (PUSH/DEPOSIT).  Returns the box index of the deposit cell,
+// or -1 when there is no shared deposit (no deposit mode, outside the box: then
+// the weights already went to global memory, or an invalid cell).
+template <int MODE>
+__device__ __forceinline__ int advance(const TileArgs &a, const Box &box, bool e_ok, const float4 *sE, int sp,
+                                       const Push32 &k, int64_t idx, P32 &s, unsigned u[8], Tally &t)
+{
+    constexpr bool kGather = MODE != MODE_DEPOSIT;
+    constexpr bool kMove = MODE == MODE_PUSH || MODE == MODE_MOVE;
+    constexpr bool kDeposit = MODE == MODE_PUSH || MODE == MODE_DEPOSIT;
+    const Geom &g = a.g;
+    int ix = cell_x(s.cell), iy = cell_y(s.cell), iz = cell_z(s.cell);
+    if (ix >= g.nx || iy >= g.ny || iz >= g.nz) {
+        flag_error(a.diag, OHPIC_ERR_BOUNDS, 3);
+        return -1;
+    }
+    if (kGather) {
+        const int key = box.key(ix, iy, iz);
+        t.out += key < 0;
+        float wx0, wx1, wy0, wy1, wz0, wz1;
+        cic<float>(a.weights, s.ox, wx0, wx1);
+        cic<float>(a.weights, s.oy, wy0, wy1);
+        cic<float>(a.weights, s.oz, wz0, wz1);
+        const float a00 = wx0 * wy0, a10 = wx1 * wy0, a01 = wx0 * wy1, a11 = wx1 * wy1;
+        const float ww[8] = {a00 * wz0, a10 * wz0, a01 * wz0, a11 * wz0, a00 * wz1, a10 * wz1, a01 * wz1, a11 * wz1};
+        float4 nd[8];
+        load_nodes<float4>(a, box, e_ok ? key : -1, ix, iy, iz, sE, nd);
+        float ex = 0.f, ey = 0.f, ez = 0.f;
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+            ex = fmaf(nd[n].x, ww[n], ex);
+            ey = fmaf(nd[n].y, ww[n], ey);
+            ez = fmaf(nd[n].z, ww[n], ez);
+        }
+        if (MODE == MODE_INTERP) {
+            double *o = a.interp_out + 3 * idx;
+            o[0] = ex;
+            o[1] = ey;
+            o[2] = ez;
+        }
+        if (kMove) {
+            // Boris rotation with per-species t and s (particle_mover_boris.f90:42-56).
+            const float hx = k.hq * ex, hy = k.hq * ey, hz = k.hq * ez;
+            const float um0 = s.vx + hx, um1 = s.vy + hy, um2 = s.vz + hz;
+            const float ua0 = um0 + (um1 * k.t2 - um2 * k.t1);
+            const float ua1 = um1 + (um2 * k.t0 - um0 * k.t2);
+            const float ua2 = um2 + (um0 * k.t1 - um1 * k.t0);
+            s.vx = um0 + (ua1 * k.s2 - ua2 * k.s1) + hx;
+            s.vy = um1 + (ua2 * k.s0 - ua0 * k.s2) + hy;
+            s.vz = um2 + (ua0 * k.s1 - ua1 * k.s0) + hz;
+            // Offset update in cell units; a crossing moves the integer cell
+            // (wrapped periodically) and keeps the offset in [0, 1).
+            float nxo = fmaf(s.vx, k.dt, s.ox), nyo = fmaf(s.vy, k.dt, s.oy), nzo = fmaf(s.vz, k.dt, s.oz);
+            float fx = floorf(nxo), fy = floorf(nyo), fz = floorf(nzo);
+            nxo -= fx; nyo -= fy; nzo -= fz;
+            if (nxo >= 1.f) { nxo = 0.f; fx += 1.f; }
+            if (nyo >= 1.f) { nyo = 0.f; fy += 1.f; }
+            if (nzo >= 1.f) { nzo = 0.f; fz += 1.f; }
+            ix += (int)fx; iy += (int)fy; iz += (int)fz;
+            if ((unsigned)ix >= (unsigned)g.nx) { ++t.cx; ix = wrapi(ix, g.nx); }
+            if ((unsigned)iy >= (unsigned)g.ny) { ++t.cy; iy = wrapi(iy, g.ny); }
+            if ((unsigned)iz >= (unsigned)g.nz) { ++t.cz; iz = wrapi(iz, g.nz); }
+            s.ox = nxo; s.oy = nyo; s.oz = nzo;
+            s.cell = pack_cell(ix, iy, iz);
+            if (a.with_energy) {
+                t.ke = fmaf(s.vx, s.vx, fmaf(s.vy, s.vy, fmaf(s.vz, s.vz, t.ke)));
+                t.px += s.vx; t.py += s.vy; t.pz += s.vz;
+            }
+        }
+    }
+    if (!kDeposit) return -1;
+    fixed_weights(a.weights, s.ox, s.oy, s.oz, u);
+    const int dkey = box.key(ix, iy, iz);
+    if (dkey < 0) {
+        deposit_global_fixed(g, a.wsum + (int64_t)sp * g.ncell, ix, iy, iz, u);
+        if (!kGather) ++t.out;
+    }
+    return dkey;
+}
+
+// Two consecutive particles per lane (8-byte vector loads and stores); the
+// pair's weights are summed in registers when both fall in one cell, then the
+// warp combines lanes sharing a cell (warp_run_deposit), a second round only
+// for pairs that split.  The next pair is loaded before the current one is
+// computed.
 template <int MODE, int DEP>
-__global__ void __launch_bounds__(256, 3) tiled_f32(TileArgs a, PartF32 p, const __grid_constant__ CUtensorMap emap)
+__global__ void __launch_bounds__(256, 2) tiled_f32(TileArgs a, PartF32 p, const __grid_constant__ CUtensorMap emap)
 {
     constexpr bool kGather = MODE != MODE_DEPOSIT;
     constexpr bool kMove = MODE == MODE_PUSH || MODE == MODE_MOVE;
     constexpr bool kDeposit = MODE == MODE_PUSH || MODE == MODE_DEPOSIT;
 
     Item it;
-    if (!get_item<1>(a, it)) return;
+    if (!get_item<2>(a, it)) return;
     const Geom &g = a.g;
     const Box box = make_box(g, it);
     extern __shared__ unsigned char smem_raw[];
@@ -248,112 +367,52 @@ __global__ void __launch_bounds__(256, 3) tiled_f32(TileArgs a, PartF32 p, const
 
     const int sp = it.sp;
     const SpeciesConst &c = a.sc[sp];
-    const float hq = (float)(c.qm * c.dt2);      // E -> half kick of the velocity
-    const float dtf = (float)c.dt;
-    const float t0 = (float)c.t[0], t1 = (float)c.t[1], t2 = (float)c.t[2];
-    const float s0 = (float)c.s[0], s1 = (float)c.s[1], s2 = (float)c.s[2];
-    unsigned ncx = 0, ncy = 0, ncz = 0, nout = 0;
-    float ke = 0.f, px = 0.f, py = 0.f, pz = 0.f;
+    Push32 k;
+    k.hq = (float)(c.qm * c.dt2);
+    k.dt = (float)c.dt;
+    k.t0 = (float)c.t[0]; k.t1 = (float)c.t[1]; k.t2 = (float)c.t[2];
+    k.s0 = (float)c.s[0]; k.s1 = (float)c.s[1]; k.s2 = (float)c.s[2];
+    const int64_t end = a.seg[sp] + a.count[sp];
+    Tally t;
 
-    int64_t i = it.g0 + threadIdx.x;
-    bool valid = i < it.g1;
-    P32 cur;
-    if (valid) load_p<kGather>(p, i, cur);
+    int64_t gi = it.g0 + threadIdx.x;
+    bool gv = gi < it.g1;
+    P32 cur[2];
+    if (gv) load_pair<kGather>(p, gi, cur);
     for (int64_t base = it.g0; base < it.g1; base += blockDim.x) {
-        const int64_t inext = i + blockDim.x;
-        const bool vnext = inext < it.g1;
-        P32 nxt;
-        if (vnext) load_p<kGather>(p, inext, nxt);
+        const int64_t gn = gi + blockDim.x;
+        const bool vn = gn < it.g1;
+        P32 nxt[2];
+        if (vn) load_pair<kGather>(p, gn, nxt);
 
-        int dkey = -1;
-        unsigned w[8];
+        int k0 = -1, k1 = -1;
+        unsigned u0[8], u1[8];
 #pragma unroll
-        for (int v = 0; v < 8; ++v) w[v] = 0u;
-        if (valid) {
-            int ix = cell_x(cur.cell), iy = cell_y(cur.cell), iz = cell_z(cur.cell);
-            bool ok = ix < g.nx && iy < g.ny && iz < g.nz;
-            if (!ok) flag_error(a.diag, OHPIC_ERR_BOUNDS, 3);
-            if (ok && kGather) {
-                const int key = box.key(ix, iy, iz);
-                nout += key < 0;
-                float wx0, wx1, wy0, wy1, wz0, wz1;
-                cic<float>(a.weights, cur.ox, wx0, wx1);
-                cic<float>(a.weights, cur.oy, wy0, wy1);
-                cic<float>(a.weights, cur.oz, wz0, wz1);
-                const float a00 = wx0 * wy0, a10 = wx1 * wy0, a01 = wx0 * wy1, a11 = wx1 * wy1;
-                const float ww[8] = {a00 * wz0, a10 * wz0, a01 * wz0, a11 * wz0,
-                                     a00 * wz1, a10 * wz1, a01 * wz1, a11 * wz1};
-                float4 nd[8];
-                load_nodes<float4>(a, box, e_ok ? key : -1, ix, iy, iz, sE, nd);
-                float ex = 0.f, ey = 0.f, ez = 0.f;
-#pragma unroll
-                for (int n = 0; n < 8; ++n) {
-                    ex = fmaf(nd[n].x, ww[n], ex);
-                    ey = fmaf(nd[n].y, ww[n], ey);
-                    ez = fmaf(nd[n].z, ww[n], ez);
-                }
-                if (MODE == MODE_INTERP) {
-                    double *o = a.interp_out + 3 * i;
-                    o[0] = ex;
-                    o[1] = ey;
-                    o[2] = ez;
-                }
-                if (kMove) {
-                    // Boris rotation with per-species t and s (particle_mover_boris.f90:42-56).
-                    const float hx = hq * ex, hy = hq * ey, hz = hq * ez;
-                    const float um0 = cur.vx + hx, um1 = cur.vy + hy, um2 = cur.vz + hz;
-                    const float ua0 = um0 + (um1 * t2 - um2 * t1);
-                    const float ua1 = um1 + (um2 * t0 - um0 * t2);
-                    const float ua2 = um2 + (um0 * t1 - um1 * t0);
-                    cur.vx = um0 + (ua1 * s2 - ua2 * s1) + hx;
-                    cur.vy = um1 + (ua2 * s0 - ua0 * s2) + hy;
-                    cur.vz = um2 + (ua0 * s1 - ua1 * s0) + hz;
-                    // Offset update in cell units; a crossing moves the integer cell
-                    // (wrapped periodically) and keeps the offset in [0, 1).
-                    float nxo = fmaf(cur.vx, dtf, cur.ox);
-                    float nyo = fmaf(cur.vy, dtf, cur.oy);
-                    float nzo = fmaf(cur.vz, dtf, cur.oz);
-                    float fx = floorf(nxo), fy = floorf(nyo), fz = floorf(nzo);
-                    nxo -= fx; nyo -= fy; nzo -= fz;
-                    if (nxo >= 1.f) { nxo = 0.f; fx += 1.f; }
-                    if (nyo >= 1.f) { nyo = 0.f; fy += 1.f; }
-                    if (nzo >= 1.f) { nzo = 0.f; fz += 1.f; }
-                    ix += (int)fx; iy += (int)fy; iz += (int)fz;
-                    if ((unsigned)ix >= (unsigned)g.nx) { ++ncx; ix = wrapi(ix, g.nx); }
-                    if ((unsigned)iy >= (unsigned)g.ny) { ++ncy; iy = wrapi(iy, g.ny); }
-                    if ((unsigned)iz >= (unsigned)g.nz) { ++ncz; iz = wrapi(iz, g.nz); }
-                    cur.ox = nxo; cur.oy = nyo; cur.oz = nzo;
-                    cur.cell = pack_cell(ix, iy, iz);
-                    if (a.with_energy) {
-                        ke = fmaf(cur.vx, cur.vx, fmaf(cur.vy, cur.vy, fmaf(cur.vz, cur.vz, ke)));
-                        px += cur.vx; py += cur.vy; pz += cur.vz;
-                    }
-                }
-            }
-            if (ok && kDeposit) {
-                fixed_weights(a.weights, cur.ox, cur.oy, cur.oz, w);
-                dkey = box.key(ix, iy, iz);
-                if (dkey < 0) {
-                    deposit_global_fixed(g, a.wsum + (int64_t)sp * g.ncell, ix, iy, iz, w);
-                    if (!kGather) ++nout;
-                }
-            }
-            if (kMove && ok) {
-                p.cell[i] = cur.cell;
-                p.ox[i] = cur.ox; p.oy[i] = cur.oy; p.oz[i] = cur.oz;
-                p.vx[i] = cur.vx; p.vy[i] = cur.vy; p.vz[i] = cur.vz;
-            }
+        for (int v = 0; v < 8; ++v) u0[v] = u1[v] = 0u;
+        if (gv) {
+            if (2 * gi < end) k0 = advance<MODE>(a, box, e_ok, sE, sp, k, 2 * gi, cur[0], u0, t);
+            if (2 * gi + 1 < end) k1 = advance<MODE>(a, box, e_ok, sE, sp, k, 2 * gi + 1, cur[1], u1, t);
+            if (kMove) store_pair(p, gi, cur);
         }
-        if (kDeposit) warp_run_deposit<DEP>(dkey, w, slo, shi, box.sx, box.sxy);
-        i = inext;
-        valid = vnext;
-        cur = nxt;
+        if (kDeposit) {
+            if (k0 >= 0 && k1 == k0) {
+#pragma unroll
+                for (int v = 0; v < 8; ++v) u0[v] += u1[v];
+                k1 = -1;
+            }
+            warp_run_deposit<DEP>(k0, u0, slo, shi, box.sx, box.sxy);
+            if (__any_sync(kFull, k1 >= 0)) warp_run_deposit<DEP>(k1, u1, slo, shi, box.sx, box.sxy);
+        }
+        gi = gn;
+        gv = vn;
+        cur[0] = nxt[0];
+        cur[1] = nxt[1];
     }
     if (kDeposit && box.on) {
         __syncthreads();
         flush_f32(a, it, slo, shi);
     }
-    if (kMove || kGather) flush_diag<float>(a, sp, ncx, ncy, ncz, nout, ke, px, py, pz);
+    if (kMove || kGather) flush_diag<float>(a, sp, t.cx, t.cy, t.cz, t.out, t.ke, t.px, t.py, t.pz);
 }
 
 }  // namespace
