@@ -240,6 +240,24 @@ int ohpic_stats(ohpic_ctx *ctx, int64_t *launches, int64_t *push_launches, doubl
 /* Device bytes held by the context. */
 int ohpic_memory(ohpic_ctx *ctx, int64_t *device_bytes);
 
+/* CIC deposit that allocates no device memory (no counterpart in the reference).
+ * For callers that cannot let a library allocate GPU memory, e.g. codes that size
+ * all device memory once through their own pool and treat a later cudaMalloc as an
+ * error.  x, y, z (n device doubles, positions in cells, wrapped periodically into
+ * [0, n); non-finite positions deposit nothing) and rho (nx*ny*nz device doubles,
+ * x fastest) are the caller's; the call adds charge * CIC(x, y, z) to rho on
+ * `stream` (a cudaStream_t, 0 = default) and returns without synchronising.
+ * Weights use the fixed-point deposit of the FP32 form (units of 2^-24 per
+ * particle, exact per-particle sum), so the result is independent of atomic order.
+ * The only scratch is a static device array of 2^21 nodes (16 MiB), held by every
+ * GPU that loads the library until the process exits; larger grids return
+ * OHPIC_ERR_CAPACITY.  The first call on a device looks up that array's device
+ * address (cudaGetSymbolAddress) with the device current.  Every call on a device
+ * shares the array and leaves it cleared, so calls that overlap on the GPU (two
+ * streams, or two host threads) race and corrupt each other's results. */
+int ohpic_scatter_noalloc(const double *x, const double *y, const double *z, int64_t n, double charge,
+                          int32_t nx, int32_t ny, int32_t nz, int32_t weights, double *rho, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

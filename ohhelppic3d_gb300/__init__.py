@@ -130,6 +130,8 @@ SIGNATURES = {
     "ohpic_memory": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "ohpic_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "ohpic_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "ohpic_scatter_noalloc": (C.c_int, [_P, _P, _P, C.c_int64, C.c_double, C.c_int32, C.c_int32, C.c_int32,
+                                        C.c_int32, _P, _P]),
 }
 
 
