@@ -38,6 +38,12 @@ PUSH_BYTES_PER_NODE = {"fp32": 12 + 4, "fp64": 24 + 8}
 # Whole-step grid term: rho write, R2C read, spectrum write, scale r/w, C2R read,
 # phi write, stencil read, E write, gather read (per node).
 STEP_BYTES_PER_NODE = {"fp32": 72, "fp64": 144}
+# DRAM traffic of one push launch over its algorithmic bytes, from one ncu capture of
+# the push (dram__bytes_read.sum + dram__bytes_write.sum) at 128x128x64 with the same
+# tile, halo and particle density (profiles/push_f32_128x128x64.md,
+# profiles/push_f64_128x128x64.md): 3.806 / 3.775 GB and 6.622 / 6.476 GB.  Both
+# terms scale with the grid at fixed density, so the ratio carries to 256^3.
+PUSH_TRAFFIC_RATIO = {"fp32": 3.806461 / 3.774873600, "fp64": 6.621735 / 6.476005376}
 
 
 def _peaks():
@@ -214,8 +220,9 @@ def run_form(P, torch, dist, wl, form, args, sampler, peak):
         "value": value, "ms_per_step": ms_max / args.steps, "particles": int(n_total),
         "roofline": {"bound": "hbm", "kernel": f"tiled_{'f32' if form == 'fp32' else 'f64'}<MODE_PUSH> (fused push)",
                      "achieved": achieved, "peak": peak[0], "unit": "GB/s", "frac": achieved / peak[0],
-                     "traffic": None, "bytes_per_launch": push_bytes, "avg_launch_ms": avg_push_ms,
-                     "peak_source": peak[1]},
+                     "traffic": PUSH_TRAFFIC_RATIO[form] * push_bytes, "bytes_per_launch": push_bytes,
+                     "avg_launch_ms": avg_push_ms, "peak_source": peak[1],
+                     "traffic_source": "ncu DRAM bytes of one push launch at 128x128x64, scaled by particles"},
         "step_hbm_frac": step_bytes / (ms_max / args.steps / 1e3) / 1e9 / peak[0],
         "push_share": st["push_ms"] / ms if ms > 0 else None,
         "gpu_launches": st["launches"] - launches0,
