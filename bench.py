@@ -266,6 +266,83 @@ def run_e2e(P, torch, dist, wl, form, args, ctx, counts):
 
 
 # ---------------------------------------------------------------------------
+# Serving: the ensemble of small runs through the continuous-batching server
+# ---------------------------------------------------------------------------
+def sequential_runs(P, reqs, sort_every: int) -> dict:
+    """One run at a time on the single-context API: create, draw, step, read the
+    diagnostics, destroy.  Times with and without the per-run set-up."""
+    import torch
+    total = steps_only = 0.0
+    work = 0
+    for r in reqs:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        caps = [c + 64 for c in _req_counts(r)]
+        cfg = P.make_config(n=r.n, dt=r.dt, b0=r.b0, qm=r.qm, q=r.q, capacity=caps, precision=P.FP32,
+                            sort_every=sort_every)
+        with P.PicContext(cfg) as ctx:
+            counts = ctx.init_particles(r.species, seed=r.seed)
+            ctx.synchronize()
+            t1 = time.perf_counter()
+            ctx.step(r.dt, r.nsteps)
+            ctx.diagnostics()
+            t2 = time.perf_counter()
+        total += time.perf_counter() - t0
+        steps_only += t2 - t1
+        work += sum(counts) * r.nsteps
+    return {"runs": len(reqs), "particle_steps": work, "seconds": total, "throughput": work / total,
+            "throughput_steps_only": work / steps_only}
+
+
+def _req_counts(r) -> list:
+    out = []
+    for sp in r.species:
+        vol = 1.0
+        for d in range(3):
+            vol *= max(min(sp.hi[d], r.n[d]) - max(sp.lo[d], 0.0), 0.0)
+        out.append(int(sp.ppc * vol) + 1)
+    return out
+
+
+def run_serving(P, args) -> dict:
+    """The ensemble workload: runs drawn from {16,24,32,48,64}^3 grids, {8,16,32,64}
+    ppc per species, wce/wpe ~ U[0,1], vth_e ~ U[0.5,2], mass ratio 100, dt 0.1,
+    steps ~ U{200..2000} x step_scale.  First all runs at once (the batched
+    capacity C), then Poisson arrivals at 0.8 C / E[work] for the p50/p99 time to
+    completion, then a sample of the same runs one at a time."""
+    from ohhelppic3d_gb300 import serve as S
+    n_runs, scale = args.serve_runs, args.serve_step_scale
+    sat_reqs = S.ensemble_stream(n_runs, rate=None, step_scale=scale)
+    with S.Server(sort_every=args.serve_sort_every) as srv:
+        sat = S.run_stream(srv, sat_reqs)
+        sat_stats = srv.stats()
+    mean_work = sat["particle_steps"] / n_runs
+    rate = 0.8 * sat["throughput"] / mean_work
+    reqs = S.ensemble_stream(n_runs, rate=rate, step_scale=scale)
+    with S.Server(sort_every=args.serve_sort_every) as srv:
+        poi = S.run_stream(srv, reqs)
+        poi_stats = srv.stats()
+    k = min(args.serve_sequential, n_runs)
+    seq = sequential_runs(P, sat_reqs[:k], args.serve_sort_every)
+    keep = ("ticks", "sort_ticks", "graph_captures", "graph_launches", "launches", "bytes_peak", "pools")
+    return {
+        "workload": (f"{n_runs} periodic FP32 runs: grids {{16,24,32,48,64}}^3, ppc per species {{8,16,32,64}}, "
+                     f"wce/wpe~U[0,1], vth_e~U[0.5,2], vth_i=vth_e/10, mass ratio 100, dt=0.1, "
+                     f"steps~U{{200..2000}} x {scale}; parameter stream pcg32 (42, 1000), run i seeded (42, 52+i)"),
+        "runs": n_runs, "step_scale": scale, "particle_steps": sat["particle_steps"],
+        "saturated": {"throughput": sat["throughput"], "span_s": sat["span_s"], "p50_s": sat["p50_s"],
+                      "p99_s": sat["p99_s"], "stats": {k2: sat_stats[k2] for k2 in keep}},
+        "poisson_80": {"rate_runs_per_s": rate, "throughput": poi["throughput"], "span_s": poi["span_s"],
+                       "p50_s": poi["p50_s"], "p99_s": poi["p99_s"], "mean_s": poi["mean_s"],
+                       "stats": {k2: poi_stats[k2] for k2 in keep}},
+        "sequential": dict(seq, how=f"the first {k} runs of the stream, one at a time on ohpic_create/"
+                                    f"ohpic_init_particles/ohpic_step/ohpic_diagnostics/ohpic_destroy"),
+        "batched_over_sequential": sat["throughput"] / seq["throughput"],
+        "unit": UNIT,
+    }
+
+
+# ---------------------------------------------------------------------------
 # CPU path (oracle): the reference's algorithm on the host cores
 # ---------------------------------------------------------------------------
 def cpu_sample_step(wl, fraction: float, threads: int, weights: int, steps: int = 1):
@@ -340,6 +417,12 @@ def main(argv=None) -> int:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n", default=None, help="grid override nx,ny,nz (same physics and ppc; for profiling)")
+    ap.add_argument("--no-serve", action="store_true", help="skip the ensemble serving measurement")
+    ap.add_argument("--serve-only", action="store_true", help="only the ensemble serving measurement")
+    ap.add_argument("--serve-runs", type=int, default=512)
+    ap.add_argument("--serve-step-scale", type=float, default=0.1)
+    ap.add_argument("--serve-sort-every", type=int, default=10)
+    ap.add_argument("--serve-sequential", type=int, default=32, help="runs timed one at a time")
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
@@ -361,6 +444,14 @@ def main(argv=None) -> int:
     peak = _peaks()
     forms = [f.strip() for f in args.forms.split(",") if f.strip()]
     sampler = ClockSampler(dist.local)
+    if args.serve_only:
+        sampler.start()
+        serving = run_serving(P, args)
+        sampler.stop()
+        if dist.rank == 0:
+            print(json.dumps({"metric": METRIC, "serving": serving, "clocks": sampler.summary()}), flush=True)
+        dist.close()
+        return 0
     results = {}
     e2e = None
     for i, form in enumerate(forms):
@@ -380,6 +471,10 @@ def main(argv=None) -> int:
         cpu = {"value": wl.nparticles / sec, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": (f"1 timed mainstep (after 1 untimed) of the oracle on {n_sample} of {wl.nparticles} "
                           f"particles over the full grid; particle time scaled to the full count, field solve once")}
+
+    serving = None
+    if not args.no_serve and dist.world == 1:
+        serving = run_serving(P, args)
 
     head = forms[0]
     r = results[head]
@@ -407,6 +502,8 @@ def main(argv=None) -> int:
                                    "step_hbm_frac": res["step_hbm_frac"], "gpu_launches": res["gpu_launches"]}
     if "fp64" in results and head == "fp32":
         line["fp32_over_fp64"] = results["fp32"]["value"] / results["fp64"]["value"]
+    if serving is not None:
+        line["serving"] = serving
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     dist.close()

@@ -78,13 +78,12 @@ __device__ __forceinline__ int wrapn(int i, int n)
     return i < 0 ? i + n : i;
 }
 
-// phi (n^3) -> padded E nodes, periodic ghosts included.
+// Padded E node t from phi (n^3), periodic ghosts included.
 template <typename T, typename NodeT>
-__global__ void k_stencil(Geom g, const T *phi, NodeT *epad)
+__device__ __forceinline__ void stencil_node(const Geom &g, const T *phi, NodeT *epad, int64_t t)
 {
-    const int64_t total = (int64_t)g.gx * g.gy * g.gz;
     const int64_t nxy = (int64_t)g.nx * g.ny;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    {
         const int px = (int)(t % g.gx);
         const int py = (int)((t / g.gx) % g.gy);
         const int pz = (int)(t / ((int64_t)g.gx * g.gy));
@@ -103,6 +102,61 @@ __global__ void k_stencil(Geom g, const T *phi, NodeT *epad)
         e.w = T(0);
         epad[t] = e;
     }
+}
+
+template <typename T, typename NodeT>
+__global__ void k_stencil(Geom g, const T *phi, NodeT *epad)
+{
+    const int64_t total = (int64_t)g.gx * g.gy * g.gz;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x)
+        stencil_node<T, NodeT>(g, phi, epad, t);
+}
+
+// ---- pooled fields: many runs of one grid size, slot = blockIdx.y; on[slot] == 0 skips ----
+
+// rho of every active slot from its fixed-point weight sums (nsp species per slot,
+// charges q[slot * nsp + s]); the sums are cleared for the next deposit.
+__global__ void k_pool_rho(unsigned long long *w, int64_t ncell, int nsp, const double *q, const int *on,
+                           float *rho)
+{
+    const int slot = blockIdx.y;
+    if (on && !on[slot]) return;
+    w += (int64_t)slot * nsp * ncell;
+    rho += (int64_t)slot * ncell;
+    q += (int64_t)slot * nsp;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ncell; t += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int s = 0; s < nsp; ++s) {
+            acc += q[s] * (double)w[s * ncell + t];
+            w[s * ncell + t] = 0ull;
+        }
+        rho[t] = (float)(acc * kWeightUnit);
+    }
+}
+
+__global__ void k_pool_scale(cufftComplex *spec, int64_t nspec, const double *green, const int *on)
+{
+    const int slot = blockIdx.y;
+    if (on && !on[slot]) return;
+    spec += (int64_t)slot * nspec;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nspec; i += (int64_t)gridDim.x * blockDim.x) {
+        const double gf = green[i];
+        cufftComplex v = spec[i];
+        v.x = (float)((double)v.x * gf);
+        v.y = (float)((double)v.y * gf);
+        spec[i] = v;
+    }
+}
+
+__global__ void k_pool_stencil(Geom g, const float *phi, float4 *epad, const int *on)
+{
+    const int slot = blockIdx.y;
+    if (on && !on[slot]) return;
+    const int64_t total = (int64_t)g.gx * g.gy * g.gz;
+    phi += (int64_t)slot * g.ncell;
+    epad += (int64_t)slot * total;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x)
+        stencil_node<float, float4>(g, phi, epad, t);
 }
 
 // One n^3 FP64 component array -> that component of every padded E node (uploaded E).
@@ -272,6 +326,61 @@ fail:
 }
 
 void launch_zero(ohpic_ctx *c, void *p, int64_t bytes) { cudaMemsetAsync(p, 0, (size_t)bytes, c->stream); }
+
+// ---- pooled solve (serve.cu): returns the number of launches, or -1 on a cuFFT error ----
+
+int pool_green(cudaStream_t st, const Geom &g, double *green)
+{
+    k_green<<<blocks_for(g.nspec), 256, 0, st>>>(g, green);
+    return 1;
+}
+
+int pool_solve(cudaStream_t st, const FieldPool &p)
+{
+    const Geom &g = p.g;
+    const unsigned slots = (unsigned)p.slots;
+    auto grid = [&](int64_t n) {
+        int64_t b = (n + 255) / 256;
+        const int64_t cap = (152 * 16 + slots - 1) / slots;
+        if (b > cap) b = cap;
+        return dim3((unsigned)(b < 1 ? 1 : b), slots);
+    };
+    k_pool_rho<<<grid(g.ncell), 256, 0, st>>>(p.wsum, g.ncell, p.nsp, p.q, p.on, p.rho);
+    if (cufftExecR2C(p.r2c, p.rho, p.spec) != CUFFT_SUCCESS) return -1;
+    k_pool_scale<<<grid(g.nspec), 256, 0, st>>>(p.spec, g.nspec, p.green, p.on);
+    if (cufftExecC2R(p.c2r, p.spec, p.phi) != CUFFT_SUCCESS) return -1;
+    k_pool_stencil<<<grid((int64_t)g.gx * g.gy * g.gz), 256, 0, st>>>(g, p.phi, p.epad, p.on);
+    return 5;
+}
+
+// rho of one slot from its weight sums (the deposit of the run's last step).
+void pool_slot_rho(cudaStream_t st, const FieldPool &p, int slot)
+{
+    const Geom &g = p.g;
+    k_pool_rho<<<dim3(blocks_for(g.ncell), 1), 256, 0, st>>>(p.wsum + (int64_t)slot * p.nsp * g.ncell, g.ncell,
+                                                             p.nsp, p.q + (int64_t)slot * p.nsp, nullptr,
+                                                             p.rho + (int64_t)slot * g.ncell);
+}
+
+// One slot's fields as FP64 arrays: rho, phi, Ex, Ey, Ez (5 * ncell doubles).
+void pool_slot_fields(cudaStream_t st, const FieldPool &p, int slot, double *dst)
+{
+    const Geom &g = p.g;
+    const int64_t n = g.ncell, npad = (int64_t)g.gx * g.gy * g.gz;
+    k_to_double<float><<<blocks_for(n), 256, 0, st>>>(p.rho + slot * n, dst, n);
+    k_to_double<float><<<blocks_for(n), 256, 0, st>>>(p.phi + slot * n, dst + n, n);
+    for (int c = 0; c < 3; ++c)
+        k_epad_component<float4><<<blocks_for(n), 256, 0, st>>>(g, p.epad + slot * npad, c, dst + (2 + c) * n);
+}
+
+// Charge and field energy of one slot (FP64 sums into d->charge, d->field_energy).
+void pool_slot_sums(cudaStream_t st, const FieldPool &p, int slot, DevDiag *d)
+{
+    const Geom &g = p.g;
+    cudaMemsetAsync(&d->charge, 0, 2 * sizeof(double), st);
+    k_field_sums<float, float4><<<blocks_for(g.ncell), 256, 0, st>>>(
+        g, p.rho + slot * g.ncell, p.epad + slot * ((int64_t)g.gx * g.gy * g.gz), &d->charge, &d->field_energy);
+}
 
 void launch_field_energy(ohpic_ctx *c)
 {

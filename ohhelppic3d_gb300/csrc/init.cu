@@ -135,48 +135,73 @@ __global__ void k_init_f32(InitArgs a, PartF32 p, uint32_t *ids)
 
 }  // namespace
 
-int init_particles(ohpic_ctx *c, uint64_t initstate, uint64_t initseq, uint64_t advance,
-                   const ohpic_species_init *spi, int64_t *counts)
+int draw_particles(const DrawSpec &d, int64_t *counts, std::string *err)
 {
-    Pcg rng = pcg_seed(initstate, initseq);
-    pcg_advance(rng, advance);
-    const int n[3] = {c->g.nx, c->g.ny, c->g.nz};
-    for (int s = 0; s < c->cfg.nspecies; ++s) {
-        const ohpic_species_init &p = spi[s];
+    Pcg rng = pcg_seed(d.initstate, d.initseq);
+    pcg_advance(rng, d.advance);
+    for (int s = 0; s < d.nspecies; ++s) {
+        const ohpic_species_init &p = d.spi[s];
         InitArgs a;
         double volume = 1.0;
-        for (int d = 0; d < 3; ++d) {
-            a.hi[d] = p.hi[d] < (double)n[d] ? p.hi[d] : (double)n[d];
-            a.lo[d] = p.lo[d] > 0.0 ? p.lo[d] : 0.0;
-            const double w = a.hi[d] - a.lo[d];
+        for (int k = 0; k < 3; ++k) {
+            a.hi[k] = p.hi[k] < (double)d.n[k] ? p.hi[k] : (double)d.n[k];
+            a.lo[k] = p.lo[k] > 0.0 ? p.lo[k] : 0.0;
+            const double w = a.hi[k] - a.lo[k];
             volume *= w > 0.0 ? w : 0.0;
-            a.drift[d] = p.drift[d];
+            a.drift[k] = p.drift[k];
         }
         // random_fix(ppc * volume): one draw decides whether the fraction rounds up.
         const double value = p.ppc * volume;
         const int64_t fixed = (int64_t)value;
         const int64_t count = pcg_double(rng) <= value - (double)fixed ? fixed + 1 : fixed;
-        if (count > c->cap[s]) {
-            c->err = "init: species " + std::to_string(s) + " needs " + std::to_string(count) + " > capacity";
+        if (d.cap && count > d.cap[s]) {
+            if (err) *err = "init: species " + std::to_string(s) + " needs " + std::to_string(count) + " > capacity";
             return OHPIC_ERR_CAPACITY;
         }
         a.base = rng;
         a.n = count;
-        a.dst = c->seg[s];
+        a.dst = d.seg ? d.seg[s] : 0;
         a.vth = p.vth;
-        a.nx = n[0]; a.ny = n[1]; a.nz = n[2];
-        if (count > 0) {
+        a.nx = d.n[0]; a.ny = d.n[1]; a.nz = d.n[2];
+        if (!d.counts_only && count > 0) {
             int64_t blocks = (count + 255) / 256;
             if (blocks > 152 * 64) blocks = 152 * 64;
-            if (c->cfg.precision == OHPIC_FP64)
-                k_init_f64<<<(unsigned)blocks, 256, 0, c->stream>>>(a, c->p64[c->cur], c->ids[c->cur]);
+            if (d.precision == OHPIC_FP64)
+                k_init_f64<<<(unsigned)blocks, 256, 0, d.stream>>>(a, d.p64, d.ids);
             else
-                k_init_f32<<<(unsigned)blocks, 256, 0, c->stream>>>(a, c->p32[c->cur], c->ids[c->cur]);
-            ++c->launches;
+                k_init_f32<<<(unsigned)blocks, 256, 0, d.stream>>>(a, d.p32, d.ids);
+            if (d.launches) ++*d.launches;
         }
         pcg_advance(rng, (uint64_t)(7 * count));
-        c->count[s] = count;
         if (counts) counts[s] = count;
+    }
+    return OHPIC_OK;
+}
+
+int init_particles(ohpic_ctx *c, uint64_t initstate, uint64_t initseq, uint64_t advance,
+                   const ohpic_species_init *spi, int64_t *counts)
+{
+    DrawSpec d;
+    d.stream = c->stream;
+    d.precision = c->cfg.precision;
+    d.n[0] = c->g.nx; d.n[1] = c->g.ny; d.n[2] = c->g.nz;
+    d.initstate = initstate;
+    d.initseq = initseq;
+    d.advance = advance;
+    d.nspecies = c->cfg.nspecies;
+    d.spi = spi;
+    d.seg = c->seg;
+    d.cap = c->cap;
+    d.p64 = c->p64[c->cur];
+    d.p32 = c->p32[c->cur];
+    d.ids = c->ids[c->cur];
+    d.launches = &c->launches;
+    int64_t cnt[OHPIC_MAX_SPECIES] = {0};
+    const int rc = draw_particles(d, cnt, &c->err);
+    if (rc != OHPIC_OK) return rc;
+    for (int s = 0; s < c->cfg.nspecies; ++s) {
+        c->count[s] = cnt[s];
+        if (counts) counts[s] = cnt[s];
     }
     c->sorted = false;
     c->rho_valid = false;

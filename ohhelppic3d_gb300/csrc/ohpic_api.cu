@@ -36,6 +36,10 @@ int default_tile(int n)
     return 1;
 }
 
+}  // namespace
+
+namespace ohpic {
+
 // Grid geometry for a tile shape and halo; false when a tile edge is not a
 // divisor of the grid or the staged box does not fit one CTA's shared memory.
 bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g)
@@ -75,6 +79,10 @@ void species_consts(const ohpic_config &cfg, int s, double dt, SpeciesConst &k)
     for (int d = 0; d < 3; ++d) k.s[d] = 2.0 * k.t[d] / (1.0 + tt);
     k.mass = k.q / k.qm;
 }
+
+}  // namespace ohpic
+
+namespace {
 
 void set_dt(ohpic_ctx *c, double dt)
 {

@@ -117,6 +117,63 @@ struct TileArgs {
     int chunk;                         // particles per CTA when unsorted
 };
 
+// One run of the multi-run push (serve.cu): its tile arguments and current particles.
+constexpr int kMaxServeRuns = 512;
+struct RunDesc {
+    TileArgs a;
+    PartF32 p;
+};
+// Arguments of the multi-run persistent push: runs[r] owns the items
+// [item_end[r-1], item_end[r]) of one queue; cursor is zero at launch.  The run
+// count is read from device memory, so a captured launch serves any set of runs.
+struct MultiPush {
+    const RunDesc *runs;
+    const int64_t *item_end;
+    const int *nruns;
+    unsigned long long *cursor;
+};
+
+// One (run, species) segment of the multi-run sort (sort.cu, driven by serve.cu).
+// Its counters are count[key_base .. key_base + ncell) in one key space shared by
+// all segments, so one exclusive scan serves every run.
+struct SortSeg {
+    Geom g;
+    PartF32 src, dst;
+    const uint32_t *ids_src;
+    uint32_t *ids_dst;
+    int64_t off, count;      // particles [off, off + count) of the run's arrays
+    int64_t key_base;
+    int64_t *tile_begin;     // ntile + 1 entries, absolute particle indices
+    DevDiag *diag;
+};
+constexpr int kMaxSortSegs = kMaxServeRuns * 2;
+constexpr int kSortChunk = 8192;   // particles per CTA pass
+struct MultiSort {
+    const SortSeg *segs;
+    const int32_t *chunk_end;   // inclusive prefix of the chunks of every segment
+    const int *nseg;            // segment count, in device memory
+    uint32_t *count;            // zeroed before the histogram
+    uint32_t *start;            // exclusive scan of count
+    uint32_t *cursor;           // zeroed before the scatter
+};
+
+// Fields of many runs of one grid size (serve.cu): slot k owns the k-th n^3 block
+// of rho and phi, the k-th spectrum and padded E, and nsp weight-sum arrays;
+// one batched cuFFT plan pair covers every slot.
+struct FieldPool {
+    Geom g;
+    int slots;
+    int nsp;                        // weight-sum arrays per slot
+    float *rho, *phi;
+    cufftComplex *spec;
+    float4 *epad;
+    unsigned long long *wsum;
+    double *green;                  // shared by the slots (same grid)
+    double *q;                      // [slot][nsp] species charges
+    int *on;                        // [slot] 1 when a run owns the slot
+    cufftHandle r2c, c2r;
+};
+
 // Host-side context.
 }  // namespace ohpic
 
@@ -193,22 +250,39 @@ struct ohpic_ctx {
 
 namespace ohpic {
 
+// Host helpers (ohpic_api.cu): geometry of a grid for a tile shape and halo
+// (false when it does not fit), and the FP64 Boris constants of one species.
+bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g);
+void species_consts(const ohpic_config &cfg, int s, double dt, SpeciesConst &k);
+
 // Kernel launchers: dispatch (convert.cu) and the two forms (push_f64.cu, push_f32.cu).
 void launch_tiled(ohpic_ctx *c, int mode, int strict);
 void launch_tiled_f64(ohpic_ctx *c, const TileArgs &a, int mode, int strict, int64_t blocks, size_t smem);
 void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks, size_t smem);
+cudaError_t launch_multi_f32(cudaStream_t st, int mode, int dep, const MultiPush &m, int grid, size_t smem);
 void ensure_emap(ohpic_ctx *c);
 // Fields (fields.cu).
 int fields_setup(ohpic_ctx *c);
 void fields_teardown(ohpic_ctx *c);
 int solve_fields(ohpic_ctx *c);
 void launch_zero(ohpic_ctx *c, void *p, int64_t bytes);
+int pool_green(cudaStream_t st, const Geom &g, double *green);
+int pool_solve(cudaStream_t st, const FieldPool &p);
+void pool_slot_rho(cudaStream_t st, const FieldPool &p, int slot);
+void pool_slot_fields(cudaStream_t st, const FieldPool &p, int slot, double *dst);
+void pool_slot_sums(cudaStream_t st, const FieldPool &p, int slot, DevDiag *d);
 void launch_field_energy(ohpic_ctx *c);
 void field_to_double(ohpic_ctx *c, int which, double *dst);
 void field_from_double(ohpic_ctx *c, int which, const double *src);
 // Sort (sort.cu).
 int sort_particles(ohpic_ctx *c);
 int64_t scan_tmp_elems(int64_t n);
+// Exclusive scan of n uint32 values; tmp holds scan_tmp_elems(n) values.
+int scan_u32(cudaStream_t st, const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp);
+// Multi-run sort passes; each returns the number of launches it made.
+int launch_sort_hist_multi(cudaStream_t st, const MultiSort &m, int64_t chunks);
+int launch_sort_finish_multi(cudaStream_t st, const MultiSort &m, int64_t chunks, int64_t max_ntile,
+                             int max_seg, int64_t nkeys, uint32_t *scan_tmp);
 // Conversions (convert.cu).
 void launch_f64_to_f32(ohpic_ctx *c, const double *stage6, int64_t n, int64_t dst, uint32_t id0,
                        int aos, int64_t stride_doubles);
@@ -219,6 +293,25 @@ void launch_kinetic(ohpic_ctx *c);
 // Device-side initial conditions (init.cu).
 int init_particles(ohpic_ctx *c, uint64_t initstate, uint64_t initseq, uint64_t advance,
                    const ohpic_species_init *spi, int64_t *counts);
+// The injector over explicit buffers: species s goes to [seg[s], seg[s] + count)
+// of p64/p32 (by precision).  counts_only draws the random_fix counts on the host
+// and launches nothing.
+struct DrawSpec {
+    cudaStream_t stream = nullptr;
+    int precision = OHPIC_FP32;
+    int n[3] = {0, 0, 0};
+    uint64_t initstate = 0, initseq = 0, advance = 0;
+    int nspecies = 0;
+    const ohpic_species_init *spi = nullptr;
+    const int64_t *seg = nullptr;
+    const int64_t *cap = nullptr;
+    PartF64 p64{};
+    PartF32 p32{};
+    uint32_t *ids = nullptr;
+    bool counts_only = false;
+    int64_t *launches = nullptr;
+};
+int draw_particles(const DrawSpec &d, int64_t *counts, std::string *err);
 
 }  // namespace ohpic
 

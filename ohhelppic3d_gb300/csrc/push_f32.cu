@@ -329,38 +329,37 @@ __device__ __forceinline__ int advance(const TileArgs &a, const Box &box, bool e
 // warp combines lanes sharing a cell (warp_run_deposit), a second round only
 // for pairs that split.  The next pair is loaded before the current one is
 // computed.
+//
+// One work item (a tile's particle range of one species) of one context.  smem
+// is the dynamic shared memory (E box, then the deposit box), ebar an mbarrier
+// for the TMA copy of the E box; emap may be null when a.use_tma is 0.
 template <int MODE, int DEP>
-__global__ void __launch_bounds__(256, 2) tiled_f32(TileArgs a, PartF32 p, const __grid_constant__ CUtensorMap emap)
+__device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap,
+                                          const Item &it, unsigned char *smem, uint64_t *ebar)
 {
     constexpr bool kGather = MODE != MODE_DEPOSIT;
     constexpr bool kMove = MODE == MODE_PUSH || MODE == MODE_MOVE;
     constexpr bool kDeposit = MODE == MODE_PUSH || MODE == MODE_DEPOSIT;
 
-    Item it;
-    if (!get_item<2>(a, it)) return;
     const Geom &g = a.g;
     const Box box = make_box(g, it);
-    extern __shared__ unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t ebar;
-    // box start aligned to 128 bytes (the launch reserves the slack)
-    unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
     const int s3 = g.sx * g.sy * g.sz;
     float4 *sE = (float4 *)smem;
     unsigned *slo = (unsigned *)(smem + (kGather ? (size_t)s3 * sizeof(float4) : 0));
     unsigned *shi = slo + s3;
     // The E box arrives by one TMA copy while the threads clear the deposit box.
-    const bool tma = box.on && kGather && a.use_tma;
+    const bool tma = box.on && kGather && a.use_tma && emap != nullptr;
     if (tma && threadIdx.x == 0) {
-        mbar_init(&ebar, 1);
-        mbar_expect_tx(&ebar, (uint32_t)(s3 * sizeof(float4)));
-        tma_load_3d(sE, &emap, 4 * it.x0, it.y0, it.z0, &ebar);
+        mbar_init(ebar, 1);
+        mbar_expect_tx(ebar, (uint32_t)(s3 * sizeof(float4)));
+        tma_load_3d(sE, emap, 4 * it.x0, it.y0, it.z0, ebar);
     }
     if (box.on) {
         stage_f32(a, it, sE, slo, shi, kGather && !tma, kDeposit);
         __syncthreads();
     }
     bool e_ok = box.on;
-    if (tma && !mbar_wait(&ebar, 0, kTmaWaitPolls)) {
+    if (tma && !mbar_wait(ebar, 0, kTmaWaitPolls)) {
         flag_error(a.diag, OHPIC_ERR_TIMEOUT, 5);
         e_ok = false;   // gather from global memory instead
     }
@@ -415,6 +414,77 @@ __global__ void __launch_bounds__(256, 2) tiled_f32(TileArgs a, PartF32 p, const
     if (kMove || kGather) flush_diag<float>(a, sp, t.cx, t.cy, t.cz, t.out, t.ke, t.px, t.py, t.pz);
 }
 
+__device__ __forceinline__ unsigned char *align128(unsigned char *p)
+{
+    return (unsigned char *)(((uintptr_t)p + 127) & ~(uintptr_t)127);
+}
+
+// One context: one CTA per work item.
+template <int MODE, int DEP>
+__global__ void __launch_bounds__(256, 2) tiled_f32(TileArgs a, PartF32 p, const __grid_constant__ CUtensorMap emap)
+{
+    Item it;
+    if (!get_item<2>(a, it)) return;
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t ebar;
+    // box start aligned to 128 bytes (the launch reserves the slack)
+    tile_pass<MODE, DEP>(a, p, &emap, it, align128(smem_raw), &ebar);
+}
+
+// Many contexts in one persistent launch.  Every CTA takes the next item from
+// one queue over all runs (an atomic cursor), looks up its run in the
+// inclusive item prefix held in shared memory, copies that run's descriptor to
+// shared memory when the run changes, and runs the same tile pass.  Runs are
+// ordered by decreasing particles per item, so the queue hands out the long
+// items first.
+template <int MODE, int DEP>
+__global__ void __launch_bounds__(256, 2) tiled_f32_multi(MultiPush m)
+{
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ __align__(16) RunDesc sd;
+    __shared__ int64_t s_end[kMaxServeRuns];
+    __shared__ int64_t s_item;
+    __shared__ int s_run;
+    __shared__ __align__(8) uint64_t ebar;
+    const int nruns = *m.nruns;
+    for (int i = threadIdx.x; i < nruns; i += blockDim.x) s_end[i] = m.item_end[i];
+    __syncthreads();
+    const int64_t total = nruns > 0 ? s_end[nruns - 1] : 0;
+    unsigned char *smem = align128(smem_raw);
+    int cur = -1;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int64_t item = (int64_t)atomicAdd(m.cursor, 1ull);
+            int lo = 0, hi = nruns - 1;
+            while (lo < hi) {   // first run whose inclusive end exceeds item
+                const int mid = (lo + hi) >> 1;
+                if (s_end[mid] > item) hi = mid;
+                else lo = mid + 1;
+            }
+            s_item = item;
+            s_run = lo;
+        }
+        __syncthreads();
+        const int64_t item = s_item;
+        const int r = s_run;
+        if (item >= total) break;
+        if (r != cur) {
+            const unsigned *src = (const unsigned *)(m.runs + r);
+            unsigned *dst = (unsigned *)&sd;
+            for (int i = threadIdx.x; i < (int)(sizeof(RunDesc) / 4); i += blockDim.x) dst[i] = src[i];
+            cur = r;
+            __syncthreads();
+        }
+        // A private copy of the descriptor: its hot fields live in registers
+        // instead of being re-read from shared memory after every shared atomic.
+        const TileArgs a = sd.a;
+        const PartF32 p = sd.p;
+        Item it;
+        if (get_item<2>(a, item - (r > 0 ? s_end[r - 1] : 0), it)) tile_pass<MODE, DEP>(a, p, nullptr, it, smem, &ebar);
+        __syncthreads();   // the next item reuses the shared boxes and descriptor
+    }
+}
+
 }  // namespace
 
 template <typename P>
@@ -448,6 +518,30 @@ void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks,
     case MODE_MOVE: launch_k(c, tiled_f32<MODE_MOVE, OHPIC_DEPOSIT_RUNS>, a, blocks, smem, pp); break;
     case MODE_INTERP: launch_k(c, tiled_f32<MODE_INTERP, OHPIC_DEPOSIT_RUNS>, a, blocks, smem, pp); break;
     }
+}
+
+template <int MODE, int DEP>
+static cudaError_t launch_multi_k(cudaStream_t st, const MultiPush &m, int grid, size_t smem)
+{
+    auto kernel = tiled_f32_multi<MODE, DEP>;
+    cudaError_t e = cudaSuccess;
+    if (smem > 48 * 1024) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kernel<<<(unsigned)grid, 256, smem, st>>>(m);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_multi_f32(cudaStream_t st, int mode, int dep, const MultiPush &m, int grid, size_t smem)
+{
+    if (grid <= 0) return cudaSuccess;
+    if (mode == MODE_DEPOSIT) {
+        if (dep == OHPIC_DEPOSIT_MATCH) return launch_multi_k<MODE_DEPOSIT, OHPIC_DEPOSIT_MATCH>(st, m, grid, smem);
+        if (dep == OHPIC_DEPOSIT_UNIFORM) return launch_multi_k<MODE_DEPOSIT, OHPIC_DEPOSIT_UNIFORM>(st, m, grid, smem);
+        return launch_multi_k<MODE_DEPOSIT, OHPIC_DEPOSIT_RUNS>(st, m, grid, smem);
+    }
+    if (dep == OHPIC_DEPOSIT_MATCH) return launch_multi_k<MODE_PUSH, OHPIC_DEPOSIT_MATCH>(st, m, grid, smem);
+    if (dep == OHPIC_DEPOSIT_UNIFORM) return launch_multi_k<MODE_PUSH, OHPIC_DEPOSIT_UNIFORM>(st, m, grid, smem);
+    return launch_multi_k<MODE_PUSH, OHPIC_DEPOSIT_RUNS>(st, m, grid, smem);
 }
 
 }  // namespace ohpic

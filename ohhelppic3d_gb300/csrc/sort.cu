@@ -154,20 +154,105 @@ __global__ void k_tile_begin(Geom g, const uint32_t *start, int64_t seg, int64_t
     if (t == g.ntile) tb[t] = seg + count;
 }
 
-// Exclusive scan of n values (in -> out) using tmp for the block sums of every level.
-void scan_exclusive(ohpic_ctx *c, const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp)
+// Exclusive scan of n values (in -> out) using tmp for the block sums of every
+// level; returns the number of launches.
+int scan_levels(cudaStream_t st, const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp)
 {
     const int64_t nb = (n + kScanBlock - 1) / kScanBlock;
     if (nb <= 1) {
-        k_scan_block<<<1, kScanThreads, 0, c->stream>>>(in, out, n, nullptr);
-        ++c->launches;
-        return;
+        k_scan_block<<<1, kScanThreads, 0, st>>>(in, out, n, nullptr);
+        return 1;
     }
     uint32_t *sums = tmp, *sums_scan = tmp + nb;
-    k_scan_block<<<(unsigned)nb, kScanThreads, 0, c->stream>>>(in, out, n, sums);
-    scan_exclusive(c, sums, sums_scan, nb, tmp + 2 * nb);
-    k_add_offsets<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(out, n, sums_scan);
-    c->launches += 2;
+    k_scan_block<<<(unsigned)nb, kScanThreads, 0, st>>>(in, out, n, sums);
+    const int inner = scan_levels(st, sums, sums_scan, nb, tmp + 2 * nb);
+    k_add_offsets<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, n, sums_scan);
+    return inner + 2;
+}
+
+void scan_exclusive(ohpic_ctx *c, const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp)
+{
+    c->launches += scan_levels(c->stream, in, out, n, tmp);
+}
+
+// ---- multi-run sort: every (run, species) segment in one pass per stage ----
+
+// Loads the inclusive chunk prefix into shared memory; returns the chunk total.
+__device__ __forceinline__ int32_t load_chunk_ends(const MultiSort &m, int32_t *s_end, int nseg)
+{
+    for (int i = threadIdx.x; i < nseg; i += blockDim.x) s_end[i] = m.chunk_end[i];
+    __syncthreads();
+    return nseg > 0 ? s_end[nseg - 1] : 0;
+}
+
+__device__ __forceinline__ int find_seg(const int32_t *s_end, int nseg, int64_t chunk)
+{
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if ((int64_t)s_end[mid] > chunk) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+__global__ void k_hist_multi(MultiSort m)
+{
+    __shared__ int32_t s_end[kMaxSortSegs];
+    const int nseg = *m.nseg;
+    const int32_t total = load_chunk_ends(m, s_end, nseg);
+    for (int64_t c = blockIdx.x; c < total; c += gridDim.x) {
+        const int si = find_seg(s_end, nseg, c);
+        const SortSeg &sg = m.segs[si];
+        const int64_t first = (c - (si > 0 ? s_end[si - 1] : 0)) * (int64_t)kSortChunk;
+        const int64_t last = min(first + (int64_t)kSortChunk, sg.count);
+        for (int64_t base = first; base < last; base += blockDim.x) {
+            const int64_t i = base + threadIdx.x;
+            const bool active = i < last;
+            const uint32_t key = active ? particle_key<true>(sg.g, PartF64{}, sg.src, sg.off + i, sg.diag) : 0u;
+            aggregated_inc(m.count + sg.key_base, key, active);
+        }
+    }
+}
+
+__global__ void k_scatter_multi(MultiSort m)
+{
+    __shared__ int32_t s_end[kMaxSortSegs];
+    const int nseg = *m.nseg;
+    const int32_t total = load_chunk_ends(m, s_end, nseg);
+    for (int64_t c = blockIdx.x; c < total; c += gridDim.x) {
+        const int si = find_seg(s_end, nseg, c);
+        const SortSeg &sg = m.segs[si];
+        const int64_t first = (c - (si > 0 ? s_end[si - 1] : 0)) * (int64_t)kSortChunk;
+        const int64_t last = min(first + (int64_t)kSortChunk, sg.count);
+        const uint32_t base0 = m.start[sg.key_base];
+        for (int64_t base = first; base < last; base += blockDim.x) {
+            const int64_t i = base + threadIdx.x;
+            const bool active = i < last;
+            const uint32_t key = active ? particle_key<true>(sg.g, PartF64{}, sg.src, sg.off + i, sg.diag) : 0u;
+            const uint32_t slot = aggregated_inc(m.cursor + sg.key_base, key, active);
+            if (!active) continue;
+            const int64_t src = sg.off + i;
+            const int64_t dst = sg.off + (int64_t)(m.start[sg.key_base + key] - base0) + slot;
+            sg.dst.cell[dst] = sg.src.cell[src];
+            sg.dst.ox[dst] = sg.src.ox[src]; sg.dst.oy[dst] = sg.src.oy[src]; sg.dst.oz[dst] = sg.src.oz[src];
+            sg.dst.vx[dst] = sg.src.vx[src]; sg.dst.vy[dst] = sg.src.vy[src]; sg.dst.vz[dst] = sg.src.vz[src];
+            if (sg.ids_src) sg.ids_dst[dst] = sg.ids_src[src];
+        }
+    }
+}
+
+// tile_begin of every segment: blockIdx.y = segment.
+__global__ void k_tile_begin_multi(MultiSort m)
+{
+    if ((int)blockIdx.y >= *m.nseg) return;
+    const SortSeg &sg = m.segs[blockIdx.y];
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nt = sg.g.ntile;
+    if (t > nt) return;
+    const uint32_t base0 = m.start[sg.key_base];
+    sg.tile_begin[t] = t == nt ? sg.off + sg.count
+                               : sg.off + (int64_t)(m.start[sg.key_base + t * sg.g.tile_cells] - base0);
 }
 
 int grid_of(int64_t n)
@@ -188,6 +273,38 @@ int64_t scan_tmp_elems(int64_t n)
         m = nb;
     }
     return total + 16;
+}
+
+int scan_u32(cudaStream_t st, const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp)
+{
+    return scan_levels(st, in, out, n, tmp);
+}
+
+int launch_sort_hist_multi(cudaStream_t st, const MultiSort &m, int64_t chunks)
+{
+    if (chunks <= 0) return 0;
+    const int64_t grid = chunks < 152 * 8 ? chunks : 152 * 8;
+    k_hist_multi<<<(unsigned)grid, 256, 0, st>>>(m);
+    return 1;
+}
+
+// Scan of the key space, tile starts, then the scatter (the cursor array must be
+// zero; the caller clears it before this call).
+int launch_sort_finish_multi(cudaStream_t st, const MultiSort &m, int64_t chunks, int64_t max_ntile,
+                             int max_seg, int64_t nkeys, uint32_t *scan_tmp)
+{
+    int launches = scan_levels(st, m.count, m.start, nkeys, scan_tmp);
+    if (max_seg > 0) {
+        dim3 grid((unsigned)((max_ntile + 1 + 255) / 256), (unsigned)max_seg);
+        k_tile_begin_multi<<<grid, 256, 0, st>>>(m);
+        ++launches;
+    }
+    if (chunks > 0) {
+        const int64_t grid = chunks < 152 * 8 ? chunks : 152 * 8;
+        k_scatter_multi<<<(unsigned)grid, 256, 0, st>>>(m);
+        ++launches;
+    }
+    return launches;
 }
 
 int sort_particles(ohpic_ctx *c)

@@ -102,10 +102,11 @@ struct Item {
     int x0, y0, z0;     // tile origin (cells)
 };
 
+// Work item b of a launch (b = blockIdx.x for a single context; the multi-run
+// kernel passes the item's index within its run).
 template <int PPT>
-__device__ __forceinline__ bool get_item(const TileArgs &a, Item &it)
+__device__ __forceinline__ bool get_item(const TileArgs &a, int64_t b, Item &it)
 {
-    const int64_t b = blockIdx.x;
     if (a.sorted) {
         const int64_t per_sp = a.g.ntile * a.split;
         it.sp = (int)(b / per_sp);
@@ -144,6 +145,12 @@ __device__ __forceinline__ bool get_item(const TileArgs &a, Item &it)
         it.x0 = it.y0 = it.z0 = 0;
     }
     return true;
+}
+
+template <int PPT>
+__device__ __forceinline__ bool get_item(const TileArgs &a, Item &it)
+{
+    return get_item<PPT>(a, (int64_t)blockIdx.x, it);
 }
 
 // Staged box: nodes (x0-halo .. x0+tx+halo) per axis, i.e. the low corners of
