@@ -219,7 +219,8 @@ int ohpic_get_stream(ohpic_ctx *ctx, void **stream);
 enum {
     OHPIC_DEPOSIT_RUNS = 0,       /* warp segmented reduction over runs of equal cells (shuffles) */
     OHPIC_DEPOSIT_UNIFORM = 1,    /* whole-warp hardware reduce when all lanes share a cell, else runs */
-    OHPIC_DEPOSIT_MATCH = 2       /* match lanes by cell, hardware reduce per group */
+    OHPIC_DEPOSIT_MATCH = 2,      /* match lanes by cell, hardware reduce per group */
+    OHPIC_DEPOSIT_GROUPS = 3      /* one whole-warp hardware reduce per distinct cell (up to 3), then runs */
 };
 typedef struct ohpic_tuning {
     int32_t tile[3];            /* cells per tile edge; powers of two dividing n, <= 64 */

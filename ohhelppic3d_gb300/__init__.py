@@ -81,7 +81,7 @@ class Tuning(C.Structure):
                 "deposit": self.deposit, "sort_every": self.sort_every}
 
 
-DEPOSIT_RUNS, DEPOSIT_UNIFORM, DEPOSIT_MATCH = 0, 1, 2
+DEPOSIT_RUNS, DEPOSIT_UNIFORM, DEPOSIT_MATCH, DEPOSIT_GROUPS = 0, 1, 2, 3
 
 
 class OhpicError(RuntimeError):

@@ -20,7 +20,7 @@ import json
 import os
 import time
 
-from . import DEPOSIT_MATCH, DEPOSIT_RUNS, DEPOSIT_UNIFORM, FP32, OhpicError, PicContext, make_config
+from . import DEPOSIT_GROUPS, DEPOSIT_MATCH, DEPOSIT_RUNS, DEPOSIT_UNIFORM, FP32, OhpicError, PicContext, make_config
 
 
 def _divisors(n: int) -> list:
@@ -114,7 +114,7 @@ def tune(n, dt, b0, qm, q, capacity_per_cell, species, precision=FP32, weights=0
 
     try:
         if precision == FP32:
-            descend("deposit", [DEPOSIT_RUNS, DEPOSIT_UNIFORM, DEPOSIT_MATCH])
+            descend("deposit", [DEPOSIT_RUNS, DEPOSIT_GROUPS, DEPOSIT_UNIFORM, DEPOSIT_MATCH])
         descend("tile", _tiles(grid))
         descend("halo", [1, 2, 3])
         if not proxy or grid == tuple(n):

@@ -751,7 +751,7 @@ int ohpic_get_tuning(ohpic_ctx *c, ohpic_tuning *t)
 int ohpic_set_tuning(ohpic_ctx *c, const ohpic_tuning *t)
 {
     if (!c || !t) return OHPIC_ERR_INVALID;
-    if (t->split < 1 || t->split > 64 || t->deposit < OHPIC_DEPOSIT_RUNS || t->deposit > OHPIC_DEPOSIT_MATCH ||
+    if (t->split < 1 || t->split > 64 || t->deposit < OHPIC_DEPOSIT_RUNS || t->deposit > OHPIC_DEPOSIT_GROUPS ||
         t->sort_every < 0)
         return fail(c, OHPIC_ERR_INVALID, "tuning: split 1..64, deposit 0..2, sort_every >= 0");
     Geom g2;

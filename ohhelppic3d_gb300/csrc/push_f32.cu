@@ -25,6 +25,8 @@
 // serialise, unlike FP32 shared atomics.  The box is flushed once per CTA into
 // per-species 64-bit global sums.  All of it is integer addition, so the deposit
 // does not depend on the order in which atomics land.
+#include <type_traits>
+
 #include "tile_common.cuh"
 #include "tma.cuh"
 
@@ -80,7 +82,26 @@ __device__ __forceinline__ void warp_run_deposit(int key, unsigned u[8], unsigne
 {
     const unsigned lane = threadIdx.x & 31u;
     bool head;
-    if (DEP == OHPIC_DEPOSIT_MATCH) {
+    if (DEP == OHPIC_DEPOSIT_GROUPS) {
+        // Cell-sorted particles put few distinct cells in a warp: reduce each of
+        // the first three over the whole warp (redux.sync, all lanes converged),
+        // the lanes left after that by runs.
+        unsigned todo = __ballot_sync(kFull, key >= 0);
+#pragma unroll 1
+        for (int round = 0; round < 3 && todo; ++round) {
+            const int leader = __ffs(todo) - 1;
+            const int k = __shfl_sync(kFull, key, leader);
+            const bool mine = key == k;
+            unsigned s[8];
+#pragma unroll
+            for (int v = 0; v < 8; ++v) s[v] = __reduce_add_sync(kFull, mine ? u[v] : 0u);
+            if ((int)lane == leader) box_add8(hi, lo, k, sx, sxy, s);
+            todo &= ~__ballot_sync(kFull, mine);
+        }
+        if (!todo) return;
+        if (!((todo >> lane) & 1u)) key = -1;
+        head = run_sum(key, u);
+    } else if (DEP == OHPIC_DEPOSIT_MATCH) {
         const unsigned peers = __match_any_sync(kFull, key);
         head = (peers & ((1u << lane) - 1u)) == 0u;
         if (peers != (1u << lane)) {
@@ -497,23 +518,33 @@ static void launch_k(ohpic_ctx *c, void (*kernel)(TileArgs, P, const CUtensorMap
     ++c->launches;
 }
 
+// The deposit strategy is a template parameter; this maps the run-time choice.
+template <int MODE, typename F>
+static auto by_deposit(int dep, F f)
+{
+    switch (dep) {
+    case OHPIC_DEPOSIT_MATCH: return f(std::integral_constant<int, OHPIC_DEPOSIT_MATCH>());
+    case OHPIC_DEPOSIT_UNIFORM: return f(std::integral_constant<int, OHPIC_DEPOSIT_UNIFORM>());
+    case OHPIC_DEPOSIT_GROUPS: return f(std::integral_constant<int, OHPIC_DEPOSIT_GROUPS>());
+    default: return f(std::integral_constant<int, OHPIC_DEPOSIT_RUNS>());
+    }
+}
+
 void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks, size_t smem)
 {
     const PartF32 &pp = c->p32[c->cur];
     switch (mode) {
     case MODE_PUSH:
-        if (a.deposit == OHPIC_DEPOSIT_MATCH)
-            launch_k(c, tiled_f32<MODE_PUSH, OHPIC_DEPOSIT_MATCH>, a, blocks, smem, pp);
-        else if (a.deposit == OHPIC_DEPOSIT_UNIFORM)
-            launch_k(c, tiled_f32<MODE_PUSH, OHPIC_DEPOSIT_UNIFORM>, a, blocks, smem, pp);
-        else launch_k(c, tiled_f32<MODE_PUSH, OHPIC_DEPOSIT_RUNS>, a, blocks, smem, pp);
+        by_deposit<MODE_PUSH>(a.deposit, [&](auto d) {
+            launch_k(c, tiled_f32<MODE_PUSH, decltype(d)::value>, a, blocks, smem, pp);
+            return 0;
+        });
         break;
     case MODE_DEPOSIT:
-        if (a.deposit == OHPIC_DEPOSIT_MATCH)
-            launch_k(c, tiled_f32<MODE_DEPOSIT, OHPIC_DEPOSIT_MATCH>, a, blocks, smem, pp);
-        else if (a.deposit == OHPIC_DEPOSIT_UNIFORM)
-            launch_k(c, tiled_f32<MODE_DEPOSIT, OHPIC_DEPOSIT_UNIFORM>, a, blocks, smem, pp);
-        else launch_k(c, tiled_f32<MODE_DEPOSIT, OHPIC_DEPOSIT_RUNS>, a, blocks, smem, pp);
+        by_deposit<MODE_DEPOSIT>(a.deposit, [&](auto d) {
+            launch_k(c, tiled_f32<MODE_DEPOSIT, decltype(d)::value>, a, blocks, smem, pp);
+            return 0;
+        });
         break;
     case MODE_MOVE: launch_k(c, tiled_f32<MODE_MOVE, OHPIC_DEPOSIT_RUNS>, a, blocks, smem, pp); break;
     case MODE_INTERP: launch_k(c, tiled_f32<MODE_INTERP, OHPIC_DEPOSIT_RUNS>, a, blocks, smem, pp); break;
@@ -534,14 +565,11 @@ static cudaError_t launch_multi_k(cudaStream_t st, const MultiPush &m, int grid,
 cudaError_t launch_multi_f32(cudaStream_t st, int mode, int dep, const MultiPush &m, int grid, size_t smem)
 {
     if (grid <= 0) return cudaSuccess;
-    if (mode == MODE_DEPOSIT) {
-        if (dep == OHPIC_DEPOSIT_MATCH) return launch_multi_k<MODE_DEPOSIT, OHPIC_DEPOSIT_MATCH>(st, m, grid, smem);
-        if (dep == OHPIC_DEPOSIT_UNIFORM) return launch_multi_k<MODE_DEPOSIT, OHPIC_DEPOSIT_UNIFORM>(st, m, grid, smem);
-        return launch_multi_k<MODE_DEPOSIT, OHPIC_DEPOSIT_RUNS>(st, m, grid, smem);
-    }
-    if (dep == OHPIC_DEPOSIT_MATCH) return launch_multi_k<MODE_PUSH, OHPIC_DEPOSIT_MATCH>(st, m, grid, smem);
-    if (dep == OHPIC_DEPOSIT_UNIFORM) return launch_multi_k<MODE_PUSH, OHPIC_DEPOSIT_UNIFORM>(st, m, grid, smem);
-    return launch_multi_k<MODE_PUSH, OHPIC_DEPOSIT_RUNS>(st, m, grid, smem);
+    if (mode == MODE_DEPOSIT)
+        return by_deposit<MODE_DEPOSIT>(
+            dep, [&](auto d) { return launch_multi_k<MODE_DEPOSIT, decltype(d)::value>(st, m, grid, smem); });
+    return by_deposit<MODE_PUSH>(
+        dep, [&](auto d) { return launch_multi_k<MODE_PUSH, decltype(d)::value>(st, m, grid, smem); });
 }
 
 }  // namespace ohpic

@@ -1118,7 +1118,7 @@ static bool normalise(const ohpic_serve_config *in, ohpic_serve_config &c)
     if (c.max_species <= 0) c.max_species = 2;
     if (c.max_species > OHPIC_MAX_SPECIES) return false;
     if (c.weights != OHPIC_WEIGHTS_REFERENCE && c.weights != OHPIC_WEIGHTS_STANDARD) return false;
-    if (c.deposit < OHPIC_DEPOSIT_RUNS || c.deposit > OHPIC_DEPOSIT_MATCH) return false;
+    if (c.deposit < OHPIC_DEPOSIT_RUNS || c.deposit > OHPIC_DEPOSIT_GROUPS) return false;
     return true;
 }
 

@@ -1,0 +1,71 @@
+"""Launch-shape tuning and the autotuner.
+
+The FP32 form deposits in integer fixed point and advances every particle on its
+own, so every launch shape must give the same state bit for bit:
+  - deposit reduction: runs, uniform, match or groups;
+  - tile shape, halo, CTAs per tile;
+  - sort cadence.
+That is what lets the autotuner pick shapes freely.  CPU tests cover the
+autotuner's candidate generation.
+"""
+import numpy as np
+import pytest
+
+
+def test_proxy_grid_and_candidate_tiles():
+    from ohhelppic3d_gb300 import autotune as A
+    assert A.proxy_grid((256, 256, 256)) == (128, 128, 64)
+    assert A.proxy_grid((32, 32, 32)) == (32, 32, 32)
+    assert A.proxy_grid((128, 128, 512)) == (128, 128, 64)
+    for n in ((256, 256, 256), (24, 24, 24), (128, 128, 512), (48, 16, 8)):
+        tiles = A._tiles(n)
+        assert tiles and all(n[d] % t[d] == 0 for t in tiles for d in range(3))
+
+
+def _run(P, tuning: dict, steps: int = 6):
+    n = (32, 32, 16)
+    ppc = 8
+    qm = [-1.0, 0.01]
+    q = [1.0 / qm[0] / ppc, 0.01 / qm[1] / ppc]
+    sp = [P.species_init(ppc, 1.4), P.species_init(ppc, 0.14)]
+    cap = [2 * ppc * n[0] * n[1] * n[2]] * 2
+    cfg = P.make_config(n=n, dt=0.1, b0=(0.0, 0.0, 0.6), qm=qm, q=q, capacity=cap, precision=P.FP32, sort_every=10)
+    with P.PicContext(cfg) as ctx:
+        if tuning:
+            ctx.set_tuning(**tuning)
+        ctx.init_particles(sp, seed=(42, 123))
+        ctx.step(0.1, steps)
+        fields = {w: ctx.field(w) for w in (P.RHO, P.PHI, P.EX, P.EY, P.EZ)}
+        parts = [ctx.download(s) for s in range(2)]
+        d = ctx.diagnostics()
+    return fields, parts, d
+
+
+@pytest.mark.gpu
+def test_fp32_state_identical_across_launch_shapes(ohpic):
+    P = ohpic
+    ref_f, ref_p, ref_d = _run(P, {})
+    variants = [{"deposit": P.DEPOSIT_UNIFORM}, {"deposit": P.DEPOSIT_MATCH}, {"deposit": P.DEPOSIT_GROUPS},
+                {"tile": (4, 4, 4)}, {"tile": (16, 8, 8), "deposit": P.DEPOSIT_GROUPS}, {"halo": 1},
+                {"halo": 3}, {"split": 3}, {"sort_every": 1}, {"sort_every": 100}]
+    for v in variants:
+        f, p, d = _run(P, v)
+        for w in f:
+            assert np.array_equal(f[w], ref_f[w]), (v, w)
+        for s in range(2):
+            for k in ("x", "y", "z", "vx", "vy", "vz"):
+                assert np.array_equal(p[s][k], ref_p[s][k]), (v, s, k)
+        assert d["crossings"] == ref_d["crossings"], v
+
+
+@pytest.mark.gpu
+def test_autotuner_returns_a_valid_shape(ohpic):
+    from ohhelppic3d_gb300 import autotune as A
+    P = ohpic
+    ppc = 8
+    sp = [P.species_init(ppc, 1.0), P.species_init(ppc, 0.1)]
+    t = A.tune(n=(32, 32, 32), dt=0.1, b0=(0.0, 0.0, 0.5), qm=[-1.0, 0.01], q=[-1.0 / ppc, 1.0 / ppc],
+               capacity_per_cell=[2 * ppc, 2 * ppc], species=sp, precision=P.FP32, steps=2, max_cadence=8)
+    assert all(32 % t["tile"][d] == 0 for d in range(3))
+    assert 0 <= t["halo"] <= 4 and t["split"] >= 1 and t["sort_every"] >= 1
+    assert t["deposit"] in (P.DEPOSIT_RUNS, P.DEPOSIT_UNIFORM, P.DEPOSIT_MATCH, P.DEPOSIT_GROUPS)
