@@ -118,17 +118,25 @@ class ClockSampler:
 # Distributed plumbing (replicas only)
 # ---------------------------------------------------------------------------
 class Dist:
+    """Replicas only: every rank runs its own copy of the workload; the ranks meet
+    only in barriers and in max/sum reductions of host timings and counts."""
+
     def __init__(self):
         self.rank = int(os.environ.get("RANK", "0"))
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.local = int(os.environ.get("LOCAL_RANK", "0"))
         self.pg = False
+        self.device = "cuda"
 
-    def init(self):
+    def init(self, backend: str = "nccl"):
         import torch
         import torch.distributed as dist
         if self.world > 1 and not dist.is_initialized():
-            dist.init_process_group("nccl", device_id=torch.device("cuda", self.local))
+            if backend == "nccl":
+                dist.init_process_group("nccl", device_id=torch.device("cuda", self.local))
+            else:
+                dist.init_process_group(backend)
+                self.device = "cpu"
             self.pg = True
 
     def barrier(self):
@@ -141,7 +149,7 @@ class Dist:
             return v
         import torch
         import torch.distributed as dist
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        t = torch.tensor([v], dtype=torch.float64, device=self.device)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
@@ -150,7 +158,7 @@ class Dist:
             return v
         import torch
         import torch.distributed as dist
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        t = torch.tensor([v], dtype=torch.float64, device=self.device)
         dist.all_reduce(t, op=dist.ReduceOp.SUM)
         return float(t.item())
 

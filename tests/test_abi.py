@@ -75,3 +75,85 @@ def test_null_arguments(ohpic):
     assert L.ohpic_destroy(None) == ohpic.OK
     assert L.ohpic_scatter(None) == ohpic.ERR_INVALID
     assert L.ohpic_step(None, 0.1, 1) == ohpic.ERR_INVALID
+
+
+_CPP_PROG = r'''
+#include <cstdio>
+#include "ohpic_modules.hpp"
+int main(int argc, char **argv)
+{
+    ohpic_config cfg;
+    ohpic_config_default(&cfg);
+    cfg.nx = cfg.ny = cfg.nz = 8;
+    cfg.nspecies = 2;
+    cfg.precision = OHPIC_FP32;
+    cfg.qm[0] = -1.0; cfg.qm[1] = 0.01;
+    cfg.q[0] = -0.125; cfg.q[1] = 0.125;
+    cfg.capacity[0] = cfg.capacity[1] = 8 * 512;
+    cfg.b0[2] = 0.5;
+    try {
+        ohpic::Context c(cfg);
+        ohpic_species_init sp[2] = {};
+        for (int s = 0; s < 2; ++s) {
+            sp[s].ppc = 4; sp[s].vth = s ? 0.1 : 1.0;
+            for (int d = 0; d < 3; ++d) sp[s].hi[d] = 1e30;
+        }
+        int64_t counts[2];
+        c.check(ohpic_init_particles(c.get(), 42, 52, 0, sp, counts), "init");
+        ohpic::FieldSolver(c).solve();
+        c.step(0.1, 2);
+        ohpic::create_particle_mover("boris", c).move_all(0.1);
+        ohpic::Scatter(c).scatter_all();
+        std::vector<double> e = ohpic::Interpolator(c).interp_all(0, counts[0]);
+        ohpic_diag d = c.diagnostics();
+        int unsupported = 0, unknown = 0;
+        try { double p[6] = {0}; double eb[6] = {0}; ohpic::create_particle_mover("boris", c).move(p, -1.0, eb, 0.1); }
+        catch (const ohpic::Error &x) { unsupported = x.status(); }
+        try { ohpic::create_particle_mover("leapfrog", c); } catch (const ohpic::Error &x) { unknown = x.status(); }
+        std::printf("ok %lld %lld %zu %d %d %.17g\n", (long long)d.count[0], (long long)d.count[1], e.size(),
+                    unsupported, unknown, d.total_charge);
+    } catch (const ohpic::Error &x) {
+        std::printf("error %d %s\n", x.status(), x.what());
+    }
+    return 0;
+}
+'''
+
+
+def _build_cpp(ohpic, tmp_path):
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no g++")
+    src = tmp_path / "mirror.cpp"
+    src.write_text(_CPP_PROG)
+    exe = tmp_path / "mirror"
+    libdir = os.path.dirname(ohpic.LIB_PATH)
+    r = subprocess.run([cxx, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                        "-L", libdir, "-lohpic", f"-Wl,-rpath,{libdir}", "-L/usr/local/cuda/lib64",
+                        "-Wl,-rpath,/usr/local/cuda/lib64"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    return out.stdout.split()
+
+
+def test_cpp_mirror_compiles_and_reports_errors(ohpic, tmp_path):
+    """The C++ mirror links against the library; without a device the context
+    constructor throws ohpic::Error carrying the status code."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible: the GPU test covers this binary")
+    words = _build_cpp(ohpic, tmp_path)
+    assert words[0] == "error" and int(words[1]) == ohpic.ERR_CUDA
+
+
+@pytest.mark.gpu
+def test_cpp_mirror_runs_the_path(ohpic, tmp_path):
+    words = _build_cpp(ohpic, tmp_path)
+    assert words[0] == "ok", words
+    n0, n1, ne, unsupported, unknown = (int(w) for w in words[1:6])
+    assert n0 == n1 == 4 * 512 and ne == 3 * n0
+    assert unsupported == ohpic.ERR_UNSUPPORTED and unknown == ohpic.ERR_INVALID
+    assert abs(float(words[6])) < 1e-9
