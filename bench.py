@@ -193,8 +193,29 @@ def timed_steps(ctx, wl, k: int, on_step=None):
             on_step()
 
 
+def tune_form(P, wl, form, args) -> dict | None:
+    """Launch shape for this workload from the autotuner, measured on a proxy grid
+    of at most 128 x 128 x 64 cells with the same particles per cell and physics
+    (the sort cadence stays the workload's)."""
+    if args.no_tune:
+        return None
+    from ohhelppic3d_gb300 import autotune
+    t0 = time.perf_counter()
+    t = autotune.tune(n=wl.n, dt=wl.dt, b0=wl.b0, qm=[s.qm for s in wl.species], q=[s.q for s in wl.species],
+                      capacity_per_cell=[s.ppc * 1.02 + 1 for s in wl.species], species=species_inits(P, wl),
+                      precision=P.FP32 if form == "fp32" else P.FP64, weights=args.weights, steps=3,
+                      max_cadence=wl.sort_every or 20)
+    keep = ("tile", "halo", "split", "deposit", "lane_particles")
+    return {**{k: t[k] for k in keep}, "tuned_on": list(t["grid_tuned_on"]), "trials": len(t["trials"]),
+            "seconds": round(time.perf_counter() - t0, 2)}
+
+
 def run_form(P, torch, dist, wl, form, args, sampler, peak):
+    tuning = tune_form(P, wl, form, args)
     ctx = make_context(P, wl, form, args.weights, dist.local)
+    if tuning:
+        from ohhelppic3d_gb300 import autotune
+        autotune.apply(ctx, tuning, keep_sort_every=True)
     counts = ctx.init_particles(species_inits(P, wl), seed=(42, 52 + dist.rank))
     n_local = sum(counts)
     ctx.sort()
@@ -234,6 +255,7 @@ def run_form(P, torch, dist, wl, form, args, sampler, peak):
         "step_hbm_frac": step_bytes / (ms_max / args.steps / 1e3) / 1e9 / peak[0],
         "push_share": st["push_ms"] / ms if ms > 0 else None,
         "gpu_launches": st["launches"] - launches0,
+        "tuning": dict(tuning or {}, applied=ctx.get_tuning()),
     }
     return ctx, counts, out
 
@@ -426,6 +448,7 @@ def main(argv=None) -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n", default=None, help="grid override nx,ny,nz (same physics and ppc; for profiling)")
     ap.add_argument("--no-serve", action="store_true", help="skip the ensemble serving measurement")
+    ap.add_argument("--no-tune", action="store_true", help="library default launch shape instead of the autotuner's")
     ap.add_argument("--serve-only", action="store_true", help="only the ensemble serving measurement")
     ap.add_argument("--serve-runs", type=int, default=512)
     ap.add_argument("--serve-step-scale", type=float, default=0.1)
@@ -497,6 +520,7 @@ def main(argv=None) -> int:
                    "l2": "inputs larger than L2 (particle state >= 30 GB per GPU)",
                    "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU"},
         "roofline": r["roofline"],
+        "tuning": r["tuning"],
         "step_hbm_frac": r["step_hbm_frac"],
         "gpu_launches": r["gpu_launches"],
         "clocks": sampler.summary(),
@@ -507,7 +531,8 @@ def main(argv=None) -> int:
         if form != head:
             line[f"{form}_form"] = {"value": res["value"], "ms_per_step": res["ms_per_step"],
                                    "dtype": "f64" if form == "fp64" else "f32", "roofline": res["roofline"],
-                                   "step_hbm_frac": res["step_hbm_frac"], "gpu_launches": res["gpu_launches"]}
+                                   "step_hbm_frac": res["step_hbm_frac"], "gpu_launches": res["gpu_launches"],
+                                   "tuning": res["tuning"]}
     if "fp64" in results and head == "fp32":
         line["fp32_over_fp64"] = results["fp32"]["value"] / results["fp64"]["value"]
     if serving is not None:

@@ -159,7 +159,8 @@ int ohpic_scatter(ohpic_ctx *ctx);
 int ohpic_solve(ohpic_ctx *ctx);
 
 /* t_Interpolator%interp over every particle of one species: e_out receives
- * 3*n doubles (Ex, Ey, Ez per particle) in device order. */
+ * 3*n doubles (Ex, Ey, Ez per particle) in device order; capacity is the number
+ * of doubles e_out holds (>= 3*n, else OHPIC_ERR_CAPACITY). */
 int ohpic_interp(ohpic_ctx *ctx, int species, double *e_out, int64_t capacity, int64_t *n_out);
 
 /* t_ParticleMover%move (Boris, particle_mover_boris.f90:21-64) followed by
@@ -228,6 +229,7 @@ typedef struct ohpic_tuning {
     int32_t split;              /* CTAs per (species, tile), 1..64 */
     int32_t deposit;            /* OHPIC_DEPOSIT_* (FP32 form) */
     int32_t sort_every;         /* cell sort cadence in steps; 0 = only explicit sorts */
+    int32_t lane_particles;     /* FP32 push: consecutive particles per lane, 2 or 4 */
 } ohpic_tuning;
 int ohpic_get_tuning(ohpic_ctx *ctx, ohpic_tuning *out);
 /* Changing tile or halo re-lays out the staged E field: the next push solves

@@ -130,7 +130,7 @@ public:
     {
         std::vector<double> e((size_t)(3 * capacity));
         int64_t n = 0;
-        c_.check(ohpic_interp(c_.get(), species, e.data(), capacity, &n), "interp");
+        c_.check(ohpic_interp(c_.get(), species, e.data(), 3 * capacity, &n), "interp");
         e.resize((size_t)(3 * n));
         return e;
     }

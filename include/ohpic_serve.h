@@ -48,7 +48,8 @@ typedef struct {
     int32_t halo;                /* staged halo cells (0 = 2) */
     int32_t deposit;             /* OHPIC_DEPOSIT_* */
     int32_t max_species;         /* species per run the pools hold (0 = 2, <= OHPIC_MAX_SPECIES) */
-    int32_t reserved[6];
+    int32_t lane_particles;      /* consecutive particles per lane in the push, 2 or 4 (0 = 4) */
+    int32_t reserved[5];
 } ohpic_serve_config;
 
 typedef struct {

@@ -30,7 +30,7 @@ def _divisors(n: int) -> list:
 def _tiles(n) -> list:
     """Candidate tile shapes: cubes and flat/tall boxes of power-of-two edges."""
     shapes = [(4, 4, 4), (8, 8, 8), (8, 8, 4), (8, 4, 4), (16, 8, 8), (16, 8, 4), (8, 8, 16), (4, 4, 8),
-              (16, 16, 4), (2, 2, 2)]
+              (16, 16, 4), (32, 8, 8), (16, 16, 8), (32, 8, 4), (2, 2, 2)]
     out = []
     for s in shapes:
         if all(n[d] % s[d] == 0 for d in range(3)) and s not in out:
@@ -114,6 +114,7 @@ def tune(n, dt, b0, qm, q, capacity_per_cell, species, precision=FP32, weights=0
 
     try:
         if precision == FP32:
+            descend("lane_particles", [2, 4])
             descend("deposit", [DEPOSIT_RUNS, DEPOSIT_GROUPS, DEPOSIT_UNIFORM, DEPOSIT_MATCH])
         descend("tile", _tiles(grid))
         descend("halo", [1, 2, 3])
@@ -144,9 +145,13 @@ def tune(n, dt, b0, qm, q, capacity_per_cell, species, precision=FP32, weights=0
     return best
 
 
-def apply(ctx: PicContext, tuning: dict):
+def apply(ctx: PicContext, tuning: dict, keep_sort_every: bool = False):
+    """Sets a tuning on a context; keep_sort_every leaves the context's cadence as is."""
+    cur = ctx.get_tuning()
     ctx.set_tuning(tile=tuning["tile"], halo=tuning["halo"], split=tuning.get("split", 1),
-                   deposit=tuning.get("deposit", DEPOSIT_RUNS), sort_every=tuning["sort_every"])
+                   deposit=tuning.get("deposit", DEPOSIT_RUNS),
+                   lane_particles=tuning.get("lane_particles", cur["lane_particles"]),
+                   sort_every=cur["sort_every"] if keep_sort_every else tuning["sort_every"])
 
 
 def save(path: str, key: str, tuning: dict):

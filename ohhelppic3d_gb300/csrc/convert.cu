@@ -157,6 +157,7 @@ void launch_tiled(ohpic_ctx *c, int mode, int strict)
     a.use_tma = c->sorted && c->emap_ok ? 1 : 0;
     a.with_energy = c->with_energy ? 1 : 0;
     a.sorted = c->sorted ? 1 : 0;
+    a.ppl = c->cfg.precision == OHPIC_FP32 && (mode == MODE_PUSH || mode == MODE_DEPOSIT) ? c->lane_particles : 2;
     a.chunk = 4096;
     for (int s = 0; s < OHPIC_MAX_SPECIES; ++s) {
         a.seg[s] = c->seg[s];

@@ -292,6 +292,7 @@ int ohpic_create(const ohpic_config *cfg, ohpic_ctx **out)
     c->with_energy = false;
     c->sc_dt = NAN;
     c->dep_strategy = OHPIC_DEPOSIT_RUNS;
+    c->lane_particles = 4;
     Geom &g = c->g;
     if (!make_geom(k, tile, c->halo, g)) {
         ohpic_destroy(c);
@@ -744,6 +745,7 @@ int ohpic_get_tuning(ohpic_ctx *c, ohpic_tuning *t)
     t->halo = c->g.halo;
     t->split = c->split;
     t->deposit = c->dep_strategy;
+    t->lane_particles = c->lane_particles;
     t->sort_every = c->cfg.sort_every;
     return OHPIC_OK;
 }
@@ -752,8 +754,9 @@ int ohpic_set_tuning(ohpic_ctx *c, const ohpic_tuning *t)
 {
     if (!c || !t) return OHPIC_ERR_INVALID;
     if (t->split < 1 || t->split > 64 || t->deposit < OHPIC_DEPOSIT_RUNS || t->deposit > OHPIC_DEPOSIT_GROUPS ||
-        t->sort_every < 0)
-        return fail(c, OHPIC_ERR_INVALID, "tuning: split 1..64, deposit 0..2, sort_every >= 0");
+        t->sort_every < 0 || (t->lane_particles != 2 && t->lane_particles != 4))
+        return fail(c, OHPIC_ERR_INVALID,
+                    "tuning: split 1..64, deposit 0..3, sort_every >= 0, lane_particles 2 or 4");
     Geom g2;
     if (!make_geom(c->cfg, t->tile, t->halo, g2))
         return fail(c, OHPIC_ERR_INVALID, "tuning: tile edges must divide the grid (<= 64) and the staged box fit");
@@ -785,6 +788,7 @@ int ohpic_set_tuning(ohpic_ctx *c, const ohpic_tuning *t)
     }
     c->split = t->split;
     c->dep_strategy = t->deposit;
+    c->lane_particles = t->lane_particles;
     c->cfg.sort_every = t->sort_every;
     return OHPIC_OK;
 }

@@ -105,6 +105,7 @@ struct TileArgs {
     int use_tma;                       // stage the E box with cp.async.bulk.tensor
     int with_energy;                   // accumulate kinetic energy / momentum
     int sorted;                        // tile_begin valid
+    int ppl;                           // FP32 push/deposit: particles per lane, 2 or 4
     int64_t seg[OHPIC_MAX_SPECIES];
     int64_t count[OHPIC_MAX_SPECIES];
     SpeciesConst sc[OHPIC_MAX_SPECIES];
@@ -235,6 +236,7 @@ struct ohpic_ctx {
     int split;
     int halo;
     int dep_strategy;           // OHPIC_DEPOSIT_* for the FP32 warp deposit
+    int lane_particles;         // FP32 push/deposit: particles per lane (2 or 4)
     bool with_energy;
     bool kin_valid;             // diag->kin holds the sums of the current velocities
 
@@ -259,7 +261,8 @@ void species_consts(const ohpic_config &cfg, int s, double dt, SpeciesConst &k);
 void launch_tiled(ohpic_ctx *c, int mode, int strict);
 void launch_tiled_f64(ohpic_ctx *c, const TileArgs &a, int mode, int strict, int64_t blocks, size_t smem);
 void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks, size_t smem);
-cudaError_t launch_multi_f32(cudaStream_t st, int mode, int dep, const MultiPush &m, int grid, size_t smem);
+cudaError_t launch_multi_f32(cudaStream_t st, int mode, int dep, int ppl, const MultiPush &m, int grid,
+                             size_t smem);
 void ensure_emap(ohpic_ctx *c);
 // Fields (fields.cu).
 int fields_setup(ohpic_ctx *c);

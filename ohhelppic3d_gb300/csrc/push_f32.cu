@@ -250,6 +250,42 @@ __device__ __forceinline__ void store_pair(const PartF32 &p, int64_t g, const P3
     *(float2 *)(p.vz + 2 * g) = make_float2(r[0].vz, r[1].vz);
 }
 
+// Particles 4g .. 4g+3: one 16-byte vector per array.
+template <bool kGather>
+__device__ __forceinline__ void load_quad(const PartF32 &p, int64_t g, P32 r[4])
+{
+    const int4 c = *(const int4 *)(p.cell + 4 * g);
+    const float4 x = *(const float4 *)(p.ox + 4 * g);
+    const float4 y = *(const float4 *)(p.oy + 4 * g);
+    const float4 z = *(const float4 *)(p.oz + 4 * g);
+    r[0].cell = c.x; r[1].cell = c.y; r[2].cell = c.z; r[3].cell = c.w;
+    r[0].ox = x.x; r[1].ox = x.y; r[2].ox = x.z; r[3].ox = x.w;
+    r[0].oy = y.x; r[1].oy = y.y; r[2].oy = y.z; r[3].oy = y.w;
+    r[0].oz = z.x; r[1].oz = z.y; r[2].oz = z.z; r[3].oz = z.w;
+    if (kGather) {
+        const float4 u = *(const float4 *)(p.vx + 4 * g);
+        const float4 v = *(const float4 *)(p.vy + 4 * g);
+        const float4 w = *(const float4 *)(p.vz + 4 * g);
+        r[0].vx = u.x; r[1].vx = u.y; r[2].vx = u.z; r[3].vx = u.w;
+        r[0].vy = v.x; r[1].vy = v.y; r[2].vy = v.z; r[3].vy = v.w;
+        r[0].vz = w.x; r[1].vz = w.y; r[2].vz = w.z; r[3].vz = w.w;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) r[j].vx = r[j].vy = r[j].vz = 0.f;
+    }
+}
+
+__device__ __forceinline__ void store_quad(const PartF32 &p, int64_t g, const P32 r[4])
+{
+    *(int4 *)(p.cell + 4 * g) = make_int4(r[0].cell, r[1].cell, r[2].cell, r[3].cell);
+    *(float4 *)(p.ox + 4 * g) = make_float4(r[0].ox, r[1].ox, r[2].ox, r[3].ox);
+    *(float4 *)(p.oy + 4 * g) = make_float4(r[0].oy, r[1].oy, r[2].oy, r[3].oy);
+    *(float4 *)(p.oz + 4 * g) = make_float4(r[0].oz, r[1].oz, r[2].oz, r[3].oz);
+    *(float4 *)(p.vx + 4 * g) = make_float4(r[0].vx, r[1].vx, r[2].vx, r[3].vx);
+    *(float4 *)(p.vy + 4 * g) = make_float4(r[0].vy, r[1].vy, r[2].vy, r[3].vy);
+    *(float4 *)(p.vz + 4 * g) = make_float4(r[0].vz, r[1].vz, r[2].vz, r[3].vz);
+}
+
 // FP32 Boris constants of one species.
 struct Push32 {
     float hq;            // qm*dt/2: E -> half kick of the velocity
@@ -435,21 +471,117 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
     if (kMove || kGather) flush_diag<float>(a, sp, t.cx, t.cy, t.cz, t.out, t.ke, t.px, t.py, t.pz);
 }
 
+// The same work item with four consecutive particles per lane (16-byte vectors,
+// PUSH and DEPOSIT only).  A lane's particles are cell-sorted neighbours, so it
+// sums their fixed-point weights in registers while the cell stays the same,
+// adds to the shared box directly when its cell changes, and the warp combines
+// the lanes' last sums once per 128 particles.  The per-particle arithmetic is
+// advance(), as in the two-per-lane pass, and every sum is integer, so both
+// passes give the same bits.
+template <int MODE, int DEP>
+__device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap,
+                                           const Item &it, unsigned char *smem, uint64_t *ebar)
+{
+    static_assert(MODE == MODE_PUSH || MODE == MODE_DEPOSIT, "four per lane: push or deposit");
+    constexpr bool kGather = MODE != MODE_DEPOSIT;
+    constexpr bool kMove = MODE == MODE_PUSH;
+
+    const Geom &g = a.g;
+    const Box box = make_box(g, it);
+    const int s3 = g.sx * g.sy * g.sz;
+    float4 *sE = (float4 *)smem;
+    unsigned *slo = (unsigned *)(smem + (kGather ? (size_t)s3 * sizeof(float4) : 0));
+    unsigned *shi = slo + s3;
+    const bool tma = box.on && kGather && a.use_tma && emap != nullptr;
+    if (tma && threadIdx.x == 0) {
+        mbar_init(ebar, 1);
+        mbar_expect_tx(ebar, (uint32_t)(s3 * sizeof(float4)));
+        tma_load_3d(sE, emap, 4 * it.x0, it.y0, it.z0, ebar);
+    }
+    if (box.on) {
+        stage_f32(a, it, sE, slo, shi, kGather && !tma, true);
+        __syncthreads();
+    }
+    bool e_ok = box.on;
+    if (tma && !mbar_wait(ebar, 0, kTmaWaitPolls)) {
+        flag_error(a.diag, OHPIC_ERR_TIMEOUT, 6);
+        e_ok = false;
+    }
+
+    const int sp = it.sp;
+    const SpeciesConst &c = a.sc[sp];
+    Push32 k;
+    k.hq = (float)(c.qm * c.dt2);
+    k.dt = (float)c.dt;
+    k.t0 = (float)c.t[0]; k.t1 = (float)c.t[1]; k.t2 = (float)c.t[2];
+    k.s0 = (float)c.s[0]; k.s1 = (float)c.s[1]; k.s2 = (float)c.s[2];
+    const int64_t end = a.seg[sp] + a.count[sp];
+    Tally t;
+
+    for (int64_t base = it.g0; base < it.g1; base += blockDim.x) {
+        const int64_t gi = base + threadIdx.x;
+        int acc_key = -1;
+        unsigned acc[8];
+#pragma unroll
+        for (int v = 0; v < 8; ++v) acc[v] = 0u;
+        if (gi < it.g1) {
+            P32 q[4];
+            load_quad<kGather>(p, gi, q);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (4 * gi + j < end) {
+                    unsigned u[8];
+                    const int kk = advance<MODE>(a, box, e_ok, sE, sp, k, 4 * gi + j, q[j], u, t);
+                    if (kk >= 0) {
+                        if (kk != acc_key) {
+                            if (acc_key >= 0) box_add8(shi, slo, acc_key, box.sx, box.sxy, acc);
+                            acc_key = kk;
+#pragma unroll
+                            for (int v = 0; v < 8; ++v) acc[v] = u[v];
+                        } else {
+#pragma unroll
+                            for (int v = 0; v < 8; ++v) acc[v] += u[v];
+                        }
+                    }
+                }
+            }
+            if (kMove) store_quad(p, gi, q);
+        }
+        warp_run_deposit<DEP>(acc_key, acc, slo, shi, box.sx, box.sxy);
+    }
+    if (box.on) {
+        __syncthreads();
+        flush_f32(a, it, slo, shi);
+    }
+    if (kGather) flush_diag<float>(a, sp, t.cx, t.cy, t.cz, t.out, t.ke, t.px, t.py, t.pz);
+}
+
 __device__ __forceinline__ unsigned char *align128(unsigned char *p)
 {
     return (unsigned char *)(((uintptr_t)p + 127) & ~(uintptr_t)127);
 }
 
-// One context: one CTA per work item.
-template <int MODE, int DEP>
-__global__ void __launch_bounds__(256, 2) tiled_f32(TileArgs a, PartF32 p, const __grid_constant__ CUtensorMap emap)
+// Work item b with PPL particles per lane: 2 (every mode) or 4 (push and deposit).
+template <int MODE, int DEP, int PPL>
+__device__ __forceinline__ void run_item(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap, int64_t b,
+                                         unsigned char *smem, uint64_t *ebar)
 {
     Item it;
-    if (!get_item<2>(a, it)) return;
+    if constexpr (PPL == 4) {
+        if (get_item<4>(a, b, it)) tile_pass4<MODE, DEP>(a, p, emap, it, smem, ebar);
+    } else {
+        if (get_item<2>(a, b, it)) tile_pass<MODE, DEP>(a, p, emap, it, smem, ebar);
+    }
+}
+
+// One context: one CTA per work item.
+template <int MODE, int DEP, int PPL>
+__global__ void __launch_bounds__(256, 2) tiled_f32(TileArgs a, PartF32 p, const __grid_constant__ CUtensorMap emap)
+{
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t ebar;
     // box start aligned to 128 bytes (the launch reserves the slack)
-    tile_pass<MODE, DEP>(a, p, &emap, it, align128(smem_raw), &ebar);
+    run_item<MODE, DEP, PPL>(a, p, &emap, (int64_t)blockIdx.x, align128(smem_raw), &ebar);
 }
 
 // Many contexts in one persistent launch.  Every CTA takes the next item from
@@ -458,7 +590,7 @@ __global__ void __launch_bounds__(256, 2) tiled_f32(TileArgs a, PartF32 p, const
 // shared memory when the run changes, and runs the same tile pass.  Runs are
 // ordered by decreasing particles per item, so the queue hands out the long
 // items first.
-template <int MODE, int DEP>
+template <int MODE, int DEP, int PPL>
 __global__ void __launch_bounds__(256, 2) tiled_f32_multi(MultiPush m)
 {
     extern __shared__ unsigned char smem_raw[];
@@ -500,8 +632,7 @@ __global__ void __launch_bounds__(256, 2) tiled_f32_multi(MultiPush m)
         // instead of being re-read from shared memory after every shared atomic.
         const TileArgs a = sd.a;
         const PartF32 p = sd.p;
-        Item it;
-        if (get_item<2>(a, item - (r > 0 ? s_end[r - 1] : 0), it)) tile_pass<MODE, DEP>(a, p, nullptr, it, smem, &ebar);
+        run_item<MODE, DEP, PPL>(a, p, nullptr, item - (r > 0 ? s_end[r - 1] : 0), smem, &ebar);
         __syncthreads();   // the next item reuses the shared boxes and descriptor
     }
 }
@@ -518,8 +649,9 @@ static void launch_k(ohpic_ctx *c, void (*kernel)(TileArgs, P, const CUtensorMap
     ++c->launches;
 }
 
-// The deposit strategy is a template parameter; this maps the run-time choice.
-template <int MODE, typename F>
+// The deposit strategy and the particles per lane are template parameters;
+// these map the run-time choices.
+template <typename F>
 static auto by_deposit(int dep, F f)
 {
     switch (dep) {
@@ -530,31 +662,36 @@ static auto by_deposit(int dep, F f)
     }
 }
 
+template <typename F>
+static auto by_lanes(int ppl, F f)
+{
+    if (ppl == 4) return f(std::integral_constant<int, 4>());
+    return f(std::integral_constant<int, 2>());
+}
+
 void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks, size_t smem)
 {
     const PartF32 &pp = c->p32[c->cur];
-    switch (mode) {
-    case MODE_PUSH:
-        by_deposit<MODE_PUSH>(a.deposit, [&](auto d) {
-            launch_k(c, tiled_f32<MODE_PUSH, decltype(d)::value>, a, blocks, smem, pp);
-            return 0;
+    if (mode == MODE_PUSH || mode == MODE_DEPOSIT) {
+        by_lanes(a.ppl, [&](auto l) {
+            return by_deposit(a.deposit, [&](auto d) {
+                constexpr int D = decltype(d)::value, L = decltype(l)::value;
+                if (mode == MODE_PUSH) launch_k(c, tiled_f32<MODE_PUSH, D, L>, a, blocks, smem, pp);
+                else launch_k(c, tiled_f32<MODE_DEPOSIT, D, L>, a, blocks, smem, pp);
+                return 0;
+            });
         });
-        break;
-    case MODE_DEPOSIT:
-        by_deposit<MODE_DEPOSIT>(a.deposit, [&](auto d) {
-            launch_k(c, tiled_f32<MODE_DEPOSIT, decltype(d)::value>, a, blocks, smem, pp);
-            return 0;
-        });
-        break;
-    case MODE_MOVE: launch_k(c, tiled_f32<MODE_MOVE, OHPIC_DEPOSIT_RUNS>, a, blocks, smem, pp); break;
-    case MODE_INTERP: launch_k(c, tiled_f32<MODE_INTERP, OHPIC_DEPOSIT_RUNS>, a, blocks, smem, pp); break;
+    } else if (mode == MODE_MOVE) {
+        launch_k(c, tiled_f32<MODE_MOVE, OHPIC_DEPOSIT_RUNS, 2>, a, blocks, smem, pp);
+    } else {
+        launch_k(c, tiled_f32<MODE_INTERP, OHPIC_DEPOSIT_RUNS, 2>, a, blocks, smem, pp);
     }
 }
 
-template <int MODE, int DEP>
+template <int MODE, int DEP, int PPL>
 static cudaError_t launch_multi_k(cudaStream_t st, const MultiPush &m, int grid, size_t smem)
 {
-    auto kernel = tiled_f32_multi<MODE, DEP>;
+    auto kernel = tiled_f32_multi<MODE, DEP, PPL>;
     cudaError_t e = cudaSuccess;
     if (smem > 48 * 1024) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -562,14 +699,17 @@ static cudaError_t launch_multi_k(cudaStream_t st, const MultiPush &m, int grid,
     return cudaGetLastError();
 }
 
-cudaError_t launch_multi_f32(cudaStream_t st, int mode, int dep, const MultiPush &m, int grid, size_t smem)
+cudaError_t launch_multi_f32(cudaStream_t st, int mode, int dep, int ppl, const MultiPush &m, int grid,
+                             size_t smem)
 {
     if (grid <= 0) return cudaSuccess;
-    if (mode == MODE_DEPOSIT)
-        return by_deposit<MODE_DEPOSIT>(
-            dep, [&](auto d) { return launch_multi_k<MODE_DEPOSIT, decltype(d)::value>(st, m, grid, smem); });
-    return by_deposit<MODE_PUSH>(
-        dep, [&](auto d) { return launch_multi_k<MODE_PUSH, decltype(d)::value>(st, m, grid, smem); });
+    return by_lanes(ppl, [&](auto l) {
+        return by_deposit(dep, [&](auto d) {
+            constexpr int D = decltype(d)::value, L = decltype(l)::value;
+            if (mode == MODE_DEPOSIT) return launch_multi_k<MODE_DEPOSIT, D, L>(st, m, grid, smem);
+            return launch_multi_k<MODE_PUSH, D, L>(st, m, grid, smem);
+        });
+    });
 }
 
 }  // namespace ohpic

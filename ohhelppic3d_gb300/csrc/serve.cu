@@ -429,6 +429,7 @@ RunDesc make_desc(const Server *s, const Run *r, int pc)
     a.use_tma = 0;
     a.with_energy = 0;
     a.sorted = 1;
+    a.ppl = s->cfg.lane_particles;
     for (int k = 0; k < r->nsp; ++k) {
         a.seg[k] = r->seg[k];
         a.count[k] = r->count[k];
@@ -614,7 +615,8 @@ int64_t enqueue_step(Server *s, int mode)
         }
     }
     cudaMemsetAsync(s->d_cursor, 0, sizeof(unsigned long long), s->st);
-    if (launch_multi_f32(s->st, mode, s->cfg.deposit, multi_push(s), s->push_grid, s->push_smem) != cudaSuccess)
+    if (launch_multi_f32(s->st, mode, s->cfg.deposit, s->cfg.lane_particles, multi_push(s), s->push_grid,
+                         s->push_smem) != cudaSuccess)
         return -1;
     return l + 2;
 }
@@ -1117,6 +1119,8 @@ static bool normalise(const ohpic_serve_config *in, ohpic_serve_config &c)
     if (c.tile < 0 || c.tile > 64) return false;
     if (c.max_species <= 0) c.max_species = 2;
     if (c.max_species > OHPIC_MAX_SPECIES) return false;
+    if (c.lane_particles == 0) c.lane_particles = 4;
+    if (c.lane_particles != 2 && c.lane_particles != 4) return false;
     if (c.weights != OHPIC_WEIGHTS_REFERENCE && c.weights != OHPIC_WEIGHTS_STANDARD) return false;
     if (c.deposit < OHPIC_DEPOSIT_RUNS || c.deposit > OHPIC_DEPOSIT_GROUPS) return false;
     return true;

@@ -47,7 +47,10 @@ def test_fp32_state_identical_across_launch_shapes(ohpic):
     ref_f, ref_p, ref_d = _run(P, {})
     variants = [{"deposit": P.DEPOSIT_UNIFORM}, {"deposit": P.DEPOSIT_MATCH}, {"deposit": P.DEPOSIT_GROUPS},
                 {"tile": (4, 4, 4)}, {"tile": (16, 8, 8), "deposit": P.DEPOSIT_GROUPS}, {"halo": 1},
-                {"halo": 3}, {"split": 3}, {"sort_every": 1}, {"sort_every": 100}]
+                {"halo": 3}, {"split": 3}, {"sort_every": 1}, {"sort_every": 100},
+                {"lane_particles": 2}, {"lane_particles": 2, "deposit": P.DEPOSIT_UNIFORM},
+                {"lane_particles": 2, "deposit": P.DEPOSIT_GROUPS, "tile": (4, 4, 4)},
+                {"lane_particles": 2, "split": 2, "halo": 1}, {"lane_particles": 2, "sort_every": 1}]
     for v in variants:
         f, p, d = _run(P, v)
         for w in f:
