@@ -192,6 +192,9 @@ void launch_tiled(ohpic_ctx *c, int mode, int strict)
     // low and high 32-bit words of the fixed-point sums (FP32).
     // (+128: the kernels align the box start to 128 bytes for TMA)
     if (a.sorted) smem = (gather ? s3 * 4 * es : 0) + (dep ? s3 * 8 : 0) + 128;
+    // four per lane (FP32 push/deposit): the boxes end on a 16-byte boundary and are
+    // followed by the per-thread prefetch stage (7 arrays x 256 threads x 16 bytes)
+    if (!f64 && a.ppl == 4) smem = (a.sorted ? ((s3 * 4 * es + s3 * 8 + 15) & ~(size_t)15) : 0) + kQuadStageBytes + 128;
     if (f64)
         launch_tiled_f64(c, a, mode, strict, blocks, smem);
     else

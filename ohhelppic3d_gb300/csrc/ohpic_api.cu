@@ -62,7 +62,8 @@ bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g)
     // Staged E box (4 reals per node) plus the deposit box (8 bytes per node).
     const int64_t s3 = (int64_t)g.sx * g.sy * g.sz;
     const int64_t es = k.precision == OHPIC_FP64 ? 8 : 4;
-    return s3 * (4 * es + 8) <= 200 * 1024;
+    // (leaves room for the FP32 push's 28 KB prefetch stage within a CTA's 227 KB)
+    return s3 * (4 * es + 8) <= 192 * 1024;
 }
 
 // Boris constants of one species for a time step (particle_mover_boris.f90:37-43),

@@ -28,6 +28,9 @@ namespace ohpic {
 
 constexpr int kSegAlign = 64;       // particles; keeps every species segment 256-B aligned
 constexpr int kMaxHalo = 4;
+// FP32 push with four particles per lane: per-thread prefetch stage in shared memory
+// (7 arrays x 256 threads x 16 bytes).
+constexpr size_t kQuadStageBytes = 7 * 256 * 16;
 // FP32-form deposit: CIC weights in units of 2^-24 (the 8 weights of a particle sum to exactly 2^24).
 constexpr float kWeightScale = 16777216.0f;
 constexpr double kWeightUnit = 1.0 / 16777216.0;

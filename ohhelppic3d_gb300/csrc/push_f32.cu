@@ -275,6 +275,55 @@ __device__ __forceinline__ void load_quad(const PartF32 &p, int64_t g, P32 r[4])
     }
 }
 
+// Prefetch of the next quad: 16-byte cp.async copies (one per array) into this
+// thread's own slots of a shared stage, so the next iteration's loads are in
+// flight during this one's arithmetic without holding registers.  The thread
+// reads back only what it copied, after cp.async.wait_group, so no block-wide
+// synchronisation is needed.  Slot of array k: st[k * blockDim.x + threadIdx.x].
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(smem_dst)), "l"(gsrc) : "memory");
+}
+
+template <bool kGather>
+__device__ __forceinline__ void prefetch_quad(float4 *st, const PartF32 &p, int64_t g)
+{
+    const int n = blockDim.x, i = threadIdx.x;
+    cp_async16(st + i, p.cell + 4 * g);
+    cp_async16(st + n + i, p.ox + 4 * g);
+    cp_async16(st + 2 * n + i, p.oy + 4 * g);
+    cp_async16(st + 3 * n + i, p.oz + 4 * g);
+    if (kGather) {
+        cp_async16(st + 4 * n + i, p.vx + 4 * g);
+        cp_async16(st + 5 * n + i, p.vy + 4 * g);
+        cp_async16(st + 6 * n + i, p.vz + 4 * g);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+template <bool kGather>
+__device__ __forceinline__ void read_quad(const float4 *st, P32 r[4])
+{
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    const int n = blockDim.x, i = threadIdx.x;
+    const float4 cf = st[i];
+    const float4 x = st[n + i], y = st[2 * n + i], z = st[3 * n + i];
+    r[0].cell = __float_as_int(cf.x); r[1].cell = __float_as_int(cf.y);
+    r[2].cell = __float_as_int(cf.z); r[3].cell = __float_as_int(cf.w);
+    r[0].ox = x.x; r[1].ox = x.y; r[2].ox = x.z; r[3].ox = x.w;
+    r[0].oy = y.x; r[1].oy = y.y; r[2].oy = y.z; r[3].oy = y.w;
+    r[0].oz = z.x; r[1].oz = z.y; r[2].oz = z.z; r[3].oz = z.w;
+    if (kGather) {
+        const float4 u = st[4 * n + i], v = st[5 * n + i], w = st[6 * n + i];
+        r[0].vx = u.x; r[1].vx = u.y; r[2].vx = u.z; r[3].vx = u.w;
+        r[0].vy = v.x; r[1].vy = v.y; r[2].vy = v.z; r[3].vy = v.w;
+        r[0].vz = w.x; r[1].vz = w.y; r[2].vz = w.z; r[3].vz = w.w;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) r[j].vx = r[j].vy = r[j].vz = 0.f;
+    }
+}
+
 __device__ __forceinline__ void store_quad(const PartF32 &p, int64_t g, const P32 r[4])
 {
     *(int4 *)(p.cell + 4 * g) = make_int4(r[0].cell, r[1].cell, r[2].cell, r[3].cell);
@@ -517,6 +566,10 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
     k.s0 = (float)c.s[0]; k.s1 = (float)c.s[1]; k.s2 = (float)c.s[2];
     const int64_t end = a.seg[sp] + a.count[sp];
     Tally t;
+    // Prefetch stage after the boxes (16-byte aligned); the launch reserves it.
+    const size_t boxes = box.on ? ((kGather ? (size_t)s3 * sizeof(float4) : 0) + (size_t)s3 * 8 + 15) & ~(size_t)15 : 0;
+    float4 *stage = (float4 *)(smem + boxes);
+    if (it.g0 + threadIdx.x < it.g1) prefetch_quad<kGather>(stage, p, it.g0 + threadIdx.x);
 
     for (int64_t base = it.g0; base < it.g1; base += blockDim.x) {
         const int64_t gi = base + threadIdx.x;
@@ -526,7 +579,8 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
         for (int v = 0; v < 8; ++v) acc[v] = 0u;
         if (gi < it.g1) {
             P32 q[4];
-            load_quad<kGather>(p, gi, q);
+            read_quad<kGather>(stage, q);
+            if (gi + blockDim.x < it.g1) prefetch_quad<kGather>(stage, p, gi + blockDim.x);
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 if (4 * gi + j < end) {

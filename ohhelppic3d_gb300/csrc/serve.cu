@@ -556,7 +556,8 @@ void fixed_shapes(Server *s)
     Geom g;
     const int n = std::max(1, 2 * std::max(1, s->cfg.tile > 0 ? s->cfg.tile : 8));
     serve_geom(s->cfg, n, n, n, g);
-    s->push_smem = (size_t)((int64_t)g.sx * g.sy * g.sz * (16 + 8) + 128);
+    s->push_smem = (size_t)((((int64_t)g.sx * g.sy * g.sz * (16 + 8) + 15) & ~(int64_t)15) + 128 +
+                            (s->cfg.lane_particles == 4 ? kQuadStageBytes : 0));
     s->push_grid = s->sms * 2;
     int64_t nt = 0;
     for (const auto &P : s->pools) nt = std::max<int64_t>(nt, P->f.g.ntile);
