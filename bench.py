@@ -40,10 +40,10 @@ PUSH_BYTES_PER_NODE = {"fp32": 12 + 4, "fp64": 24 + 8}
 STEP_BYTES_PER_NODE = {"fp32": 72, "fp64": 144}
 # DRAM traffic of one push launch over its algorithmic bytes, from one ncu capture of
 # the push (dram__bytes_read.sum + dram__bytes_write.sum) at 128x128x64 with the same
-# tile, halo and particle density (profiles/push_f32_128x128x64.md,
-# profiles/push_f64_128x128x64.md): 3.806 / 3.775 GB and 6.622 / 6.476 GB.  Both
+# tuned tile, halo and particle density (profiles/push_f32_128x128x64.md,
+# profiles/push_f64_128x128x64.md): 3.794 / 3.775 GB and 6.622 / 6.476 GB.  Both
 # terms scale with the grid at fixed density, so the ratio carries to 256^3.
-PUSH_TRAFFIC_RATIO = {"fp32": 3.806461 / 3.774873600, "fp64": 6.621735 / 6.476005376}
+PUSH_TRAFFIC_RATIO = {"fp32": 3.793867 / 3.774873600, "fp64": 6.621735 / 6.476005376}
 
 
 def _peaks():
@@ -197,6 +197,8 @@ def tune_form(P, wl, form, args) -> dict | None:
     """Launch shape for this workload from the autotuner, measured on a proxy grid
     of at most 128 x 128 x 64 cells with the same particles per cell and physics
     (the sort cadence stays the workload's)."""
+    if args.tuning:
+        return dict(json.loads(args.tuning), tuned_on="given on the command line")
     if args.no_tune:
         return None
     from ohhelppic3d_gb300 import autotune
@@ -449,6 +451,8 @@ def main(argv=None) -> int:
     ap.add_argument("--n", default=None, help="grid override nx,ny,nz (same physics and ppc; for profiling)")
     ap.add_argument("--no-serve", action="store_true", help="skip the ensemble serving measurement")
     ap.add_argument("--no-tune", action="store_true", help="library default launch shape instead of the autotuner's")
+    ap.add_argument("--tuning", default=None,
+                    help='fixed launch shape instead of the autotuner, e.g. \'{"tile": [16, 8, 8], "halo": 1}\'')
     ap.add_argument("--serve-only", action="store_true", help="only the ensemble serving measurement")
     ap.add_argument("--serve-runs", type=int, default=512)
     ap.add_argument("--serve-step-scale", type=float, default=0.1)

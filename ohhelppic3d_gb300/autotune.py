@@ -148,10 +148,10 @@ def tune(n, dt, b0, qm, q, capacity_per_cell, species, precision=FP32, weights=0
 def apply(ctx: PicContext, tuning: dict, keep_sort_every: bool = False):
     """Sets a tuning on a context; keep_sort_every leaves the context's cadence as is."""
     cur = ctx.get_tuning()
-    ctx.set_tuning(tile=tuning["tile"], halo=tuning["halo"], split=tuning.get("split", 1),
-                   deposit=tuning.get("deposit", DEPOSIT_RUNS),
+    ctx.set_tuning(tile=tuning.get("tile", cur["tile"]), halo=tuning.get("halo", cur["halo"]),
+                   split=tuning.get("split", cur["split"]), deposit=tuning.get("deposit", cur["deposit"]),
                    lane_particles=tuning.get("lane_particles", cur["lane_particles"]),
-                   sort_every=cur["sort_every"] if keep_sort_every else tuning["sort_every"])
+                   sort_every=cur["sort_every"] if keep_sort_every else tuning.get("sort_every", cur["sort_every"]))
 
 
 def save(path: str, key: str, tuning: dict):
