@@ -9,7 +9,7 @@
 // fixed-point weight sums, is the file-scope array below.  Every GPU that loads
 // the library holds it (16 MiB) until the process exits.
 //
-// Algorithm: the same fixed-point CIC deposit as the FP32 form's shared box
+// Algorithm: a fixed-point CIC deposit like the FP32 form's shared box
 // (push_f32.cu).  Each particle's 8 weights are rounded to units of 2^-24, the
 // largest corner takes the rounding remainder so they sum to exactly 2^24, and
 // they are added with 64-bit integer atomics.  A second kernel adds

@@ -16,8 +16,8 @@
 // stores are 8-byte vector accesses coalesced across the warp; the next pair's
 // 7 vectors are loaded before the current pair is computed.
 //
-// Deposit in fixed point.  Each particle's 8 CIC weights are rounded to units of
-// 2^-24 with the largest one adjusted so they sum to exactly 2^24 (charge is
+// Deposit in fixed point.  Each particle's 8 CIC weights are integers in units of
+// 2^-24 that sum to exactly 2^24 (an exact axis-by-axis split; charge is
 // conserved exactly).  A warp segmented reduction (integer shuffles, at most 5
 // steps, stopping early when runs are short) sums each run into its first lane,
 // which adds the sums to a shared 64-bit box kept as 32-bit low/high words:
@@ -123,28 +123,27 @@ __device__ __forceinline__ void warp_run_deposit(int key, unsigned u[8], unsigne
     if (head && key >= 0) box_add8(hi, lo, key, sx, sxy, u);
 }
 
-// CIC weights of one particle in units of 2^-24, summing to exactly 2^24: the
-// largest corner (the product of the larger weight on each axis, >= 1/8) takes
-// the rounding remainder.
+// CIC weights of one particle in units of 2^-24, summing to exactly 2^24.  The
+// total is split exactly, one axis at a time: x into X1 = round(wx1 * 2^24) and
+// X0 = 2^24 - X1, each half into y parts, each quarter into z parts.  A child is
+// rounded from its parent's FP32 product and clamped to the parent's integer, the
+// sibling is the difference, so every weight is non-negative and the eight add
+// up to 2^24 with no fix-up pass (7 float-to-integer conversions instead of 8).
 __device__ __forceinline__ void fixed_weights(int conv, float ox, float oy, float oz, unsigned u[8])
 {
     float wx0, wx1, wy0, wy1, wz0, wz1;
     cic<float>(conv, ox, wx0, wx1);
     cic<float>(conv, oy, wy0, wy1);
     cic<float>(conv, oz, wz0, wz1);
-    const float a00 = wx0 * wy0, a10 = wx1 * wy0, a01 = wx0 * wy1, a11 = wx1 * wy1;
-    const float sz0 = wz0 * kWeightScale, sz1 = wz1 * kWeightScale;   // exact: power-of-two scale
-    const float f[8] = {a00 * sz0, a10 * sz0, a01 * sz0, a11 * sz0, a00 * sz1, a10 * sz1, a01 * sz1, a11 * sz1};
-    unsigned sum = 0;
-#pragma unroll
-    for (int v = 0; v < 8; ++v) {
-        u[v] = __float2uint_rn(f[v]);
-        sum += u[v];
-    }
-    const int big = (wx1 > wx0 ? 1 : 0) + (wy1 > wy0 ? 2 : 0) + (wz1 > wz0 ? 4 : 0);
-    const unsigned fix = (1u << 24) - sum;   // small, possibly "negative" (mod 2^32)
-#pragma unroll
-    for (int v = 0; v < 8; ++v) u[v] += v == big ? fix : 0u;
+    const float fx1 = wx1 * kWeightScale, fx0 = wx0 * kWeightScale;   // exact: power-of-two scale
+    const unsigned X1 = __float2uint_rn(fx1), X0 = (1u << 24) - X1;
+    const float f11 = fx1 * wy1, f01 = fx0 * wy1, f10 = fx1 * wy0, f00 = fx0 * wy0;
+    const unsigned Y11 = min(__float2uint_rn(f11), X1), Y01 = min(__float2uint_rn(f01), X0);
+    const unsigned Y10 = X1 - Y11, Y00 = X0 - Y01;
+    const unsigned Z00 = min(__float2uint_rn(f00 * wz1), Y00), Z10 = min(__float2uint_rn(f10 * wz1), Y10);
+    const unsigned Z01 = min(__float2uint_rn(f01 * wz1), Y01), Z11 = min(__float2uint_rn(f11 * wz1), Y11);
+    u[0] = Y00 - Z00; u[1] = Y10 - Z10; u[2] = Y01 - Z01; u[3] = Y11 - Z11;
+    u[4] = Z00; u[5] = Z10; u[6] = Z01; u[7] = Z11;
 }
 
 __device__ __forceinline__ void deposit_global_fixed(const Geom &g, unsigned long long *w, int ix, int iy, int iz,
