@@ -206,9 +206,10 @@ def tune_form(P, wl, form, args) -> dict | None:
     t = autotune.tune(n=wl.n, dt=wl.dt, b0=wl.b0, qm=[s.qm for s in wl.species], q=[s.q for s in wl.species],
                       capacity_per_cell=[s.ppc * 1.02 + 1 for s in wl.species], species=species_inits(P, wl),
                       precision=P.FP32 if form == "fp32" else P.FP64, weights=args.weights, steps=3,
-                      max_cadence=wl.sort_every or 20)
+                      max_cadence=40)
     keep = ("tile", "halo", "split", "deposit", "lane_particles")
-    return {**{k: t[k] for k in keep}, "tuned_on": list(t["grid_tuned_on"]), "trials": len(t["trials"]),
+    return {**{k: t[k] for k in keep}, "sort_every_suggested": t["sort_every"],
+            "tuned_on": list(t["grid_tuned_on"]), "trials": len(t["trials"]),
             "seconds": round(time.perf_counter() - t0, 2)}
 
 
@@ -258,6 +259,7 @@ def run_form(P, torch, dist, wl, form, args, sampler, peak):
         "push_share": st["push_ms"] / ms if ms > 0 else None,
         "gpu_launches": st["launches"] - launches0,
         "tuning": dict(tuning or {}, applied=ctx.get_tuning()),
+        "sort_every": wl.sort_every,
     }
     return ctx, counts, out
 
@@ -313,6 +315,7 @@ def sequential_runs(P, reqs, sort_every: int) -> dict:
         cfg = P.make_config(n=r.n, dt=r.dt, b0=r.b0, qm=r.qm, q=r.q, capacity=caps, precision=P.FP32,
                             sort_every=sort_every)
         with P.PicContext(cfg) as ctx:
+            ctx.set_tuning(halo=1)   # the server's launch shape
             counts = ctx.init_particles(r.species, seed=r.seed)
             ctx.synchronize()
             t1 = time.perf_counter()
@@ -456,7 +459,7 @@ def main(argv=None) -> int:
     ap.add_argument("--serve-only", action="store_true", help="only the ensemble serving measurement")
     ap.add_argument("--serve-runs", type=int, default=512)
     ap.add_argument("--serve-step-scale", type=float, default=0.1)
-    ap.add_argument("--serve-sort-every", type=int, default=10)
+    ap.add_argument("--serve-sort-every", type=int, default=20)
     ap.add_argument("--serve-sequential", type=int, default=32, help="runs timed one at a time")
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "ours":
@@ -520,8 +523,9 @@ def main(argv=None) -> int:
         "data": "synthetic: device-side pcg32 injector, seeds (42, 52 + rank), Maxwellian velocities",
         "config": {"workload": wl.description, "form": {"fp32": "FP32 precision form (int32 cell + FP32 offset)",
                                                         "fp64": "plain FP64 form"}[head],
-                   "weights": _wname(args.weights), "particles": r["particles"],
-                   "l2": "inputs larger than L2 (particle state >= 30 GB per GPU)",
+                   "weights": _wname(args.weights), "particles": r["particles"], "sort_every": r["sort_every"],
+                   "l2": (f"inputs larger than L2: {r['particles'] * (28 if head == 'fp32' else 48) / 1e9:.1f} GB "
+                          f"of particle state per GPU against a 129 MB L2"),
                    "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU"},
         "roofline": r["roofline"],
         "tuning": r["tuning"],

@@ -41,11 +41,12 @@ typedef struct {
     int32_t max_active;          /* runs on the GPU at once (<= 512; 0 = 512) */
     int64_t hbm_budget;          /* bytes for run state and field pools (0 = 60% of free memory) */
     int32_t slots_per_pool;      /* field slots per grid-size pool (0 = 16) */
-    int32_t sort_every;          /* ticks between cell sorts of all runs (0 = 10) */
+    int32_t sort_every;          /* ticks between cell sorts of all runs (0 = 20) */
     int32_t use_graphs;          /* 1: replay each tick as a captured CUDA graph */
     int32_t weights;             /* OHPIC_WEIGHTS_* for every run */
-    int32_t tile;                /* tile edge in cells (0 = 8, or the largest power of two <= 8 dividing n) */
-    int32_t halo;                /* staged halo cells (0 = 2) */
+    int32_t tile;                /* largest tile edge in cells (0 = 8); per grid, the largest power of two
+                                    <= tile dividing the edge */
+    int32_t halo;                /* staged halo cells (0 = 1) */
     int32_t deposit;             /* OHPIC_DEPOSIT_* */
     int32_t max_species;         /* species per run the pools hold (0 = 2, <= OHPIC_MAX_SPECIES) */
     int32_t lane_particles;      /* consecutive particles per lane in the push, 2 or 4 (0 = 4) */

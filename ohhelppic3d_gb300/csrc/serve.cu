@@ -64,10 +64,13 @@ constexpr int kStageSlots = 4;     // pinned staging buffers for table uploads
 
 int64_t align256(int64_t v) { return (v + 255) & ~(int64_t)255; }
 
+// Tile edge for a grid edge n: the largest power of two <= want (8 when want is 0)
+// that divides n, so one setting serves every grid size.
 int pick_tile(int n, int want)
 {
-    if (want > 0) return n % want == 0 ? want : -1;
-    for (int t = 8; t > 1; t >>= 1)
+    int t = 1;
+    while (2 * t <= (want > 0 ? want : 8)) t *= 2;
+    for (; t > 1; t >>= 1)
         if (n % t == 0) return t;
     return 1;
 }
@@ -1080,10 +1083,10 @@ void ohpic_serve_config_default(ohpic_serve_config *cfg)
     memset(cfg, 0, sizeof(*cfg));
     cfg->max_active = kMaxServeRuns;
     cfg->slots_per_pool = 16;
-    cfg->sort_every = 10;
+    cfg->sort_every = 20;
     cfg->use_graphs = 1;
     cfg->weights = OHPIC_WEIGHTS_REFERENCE;
-    cfg->halo = 2;
+    cfg->halo = 1;
     cfg->deposit = OHPIC_DEPOSIT_RUNS;
     cfg->max_species = 2;
 }
@@ -1114,8 +1117,8 @@ static bool normalise(const ohpic_serve_config *in, ohpic_serve_config &c)
     if (c.slots_per_pool <= 0) c.slots_per_pool = 16;
     if (c.slots_per_pool > 256) return false;
     if (c.sort_every < 0) return false;
-    if (c.sort_every == 0) c.sort_every = 10;
-    if (c.halo <= 0) c.halo = 2;
+    if (c.sort_every == 0) c.sort_every = 20;
+    if (c.halo <= 0) c.halo = 1;
     if (c.halo > kMaxHalo) return false;
     if (c.tile < 0 || c.tile > 64) return false;
     if (c.max_species <= 0) c.max_species = 2;
@@ -1241,7 +1244,11 @@ int ohpic_serve_submit(ohpic_server *s, const ohpic_run_request *req, int64_t *i
     if (!s || !req) return OHPIC_ERR_INVALID;
     std::unique_ptr<Run> r(new (std::nothrow) Run());
     if (!r) return OHPIC_ERR_OOM;
-    if (!plan_run(s->cfg, *req, *r)) return OHPIC_ERR_INVALID;
+    if (!plan_run(s->cfg, *req, *r)) {
+        s->set_err("submit: invalid request (grid 2..2048 x 2048 x 1024, 1..max_species species, finite "
+                   "non-zero qm, nsteps >= 1) or a staged tile box too large for shared memory");
+        return OHPIC_ERR_INVALID;
+    }
     if (r->bytes + pool_bytes(r->g, s->cfg.slots_per_pool, s->cfg.max_species) > s->cfg.hbm_budget)
         return OHPIC_ERR_CAPACITY;
     std::lock_guard<std::mutex> lk(s->mu);
