@@ -103,6 +103,63 @@ __global__ void k_f32_to_stage(PartF32 p, int64_t src, int64_t n, double *stage)
     }
 }
 
+// Direct forms: the six FP64 arrays are the caller's host arrays, read or written
+// by the kernel itself.  Pinned host memory is reachable from the GPU at the same
+// address (over NVLink-C2C on Grace), so no device staging copy is needed.
+__global__ void k_soa_to_f32(Soa6 s, int64_t n, PartF32 p, uint32_t *ids, int64_t dst, uint32_t id0, int nx, int ny,
+                             int nz, DevDiag *d)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int ix, iy, iz;
+        float ox, oy, oz;
+        split_pos(s.p[0][i], nx, ix, ox, d);
+        split_pos(s.p[1][i], ny, iy, oy, d);
+        split_pos(s.p[2][i], nz, iz, oz, d);
+        const int64_t o = dst + i;
+        p.cell[o] = pack_cell(ix, iy, iz);
+        p.ox[o] = ox; p.oy[o] = oy; p.oz[o] = oz;
+        p.vx[o] = (float)s.p[3][i]; p.vy[o] = (float)s.p[4][i]; p.vz[o] = (float)s.p[5][i];
+        if (ids) ids[o] = id0 + (uint32_t)i;
+    }
+}
+
+__global__ void k_soa_to_f64(Soa6 s, int64_t n, PartF64 p, uint32_t *ids, int64_t dst, uint32_t id0)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t o = dst + i;
+        p.x[o] = s.p[0][i]; p.y[o] = s.p[1][i]; p.z[o] = s.p[2][i];
+        p.vx[o] = s.p[3][i]; p.vy[o] = s.p[4][i]; p.vz[o] = s.p[5][i];
+        if (ids) ids[o] = id0 + (uint32_t)i;
+    }
+}
+
+__global__ void k_f32_to_soa(PartF32 p, int64_t src, int64_t n, Soa6w out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t o = src + i;
+        const int32_t c = p.cell[o];
+        if (out.p[0]) out.p[0][i] = (double)cell_x(c) + (double)p.ox[o];
+        if (out.p[1]) out.p[1][i] = (double)cell_y(c) + (double)p.oy[o];
+        if (out.p[2]) out.p[2][i] = (double)cell_z(c) + (double)p.oz[o];
+        if (out.p[3]) out.p[3][i] = p.vx[o];
+        if (out.p[4]) out.p[4][i] = p.vy[o];
+        if (out.p[5]) out.p[5][i] = p.vz[o];
+    }
+}
+
+__global__ void k_f64_to_soa(PartF64 p, int64_t src, int64_t n, Soa6w out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t o = src + i;
+        if (out.p[0]) out.p[0][i] = p.x[o];
+        if (out.p[1]) out.p[1][i] = p.y[o];
+        if (out.p[2]) out.p[2][i] = p.z[o];
+        if (out.p[3]) out.p[3][i] = p.vx[o];
+        if (out.p[4]) out.p[4][i] = p.vy[o];
+        if (out.p[5]) out.p[5][i] = p.vz[o];
+    }
+}
+
 // Kinetic energy and momentum of every species (FP64 accumulation).
 template <bool F32>
 __global__ void k_kinetic(PartF64 p64, PartF32 p32, int64_t seg, int64_t n, double *out4)
@@ -217,6 +274,27 @@ void launch_f64_to_f32(ohpic_ctx *c, const double *stage, int64_t n, int64_t dst
     k_stage_to_f32<<<grid_for(n, 256), 256, 0, c->stream>>>(stage, n, aos, stride_doubles, c->p32[c->cur],
                                                              c->ids[c->cur], dst, id0, c->g.nx, c->g.ny,
                                                              c->g.nz, c->diag);
+    ++c->launches;
+}
+
+void launch_from_host_soa(ohpic_ctx *c, const Soa6 &s, int64_t n, int64_t dst, uint32_t id0)
+{
+    if (n <= 0) return;
+    if (c->cfg.precision == OHPIC_FP64)
+        k_soa_to_f64<<<grid_for(n, 256), 256, 0, c->stream>>>(s, n, c->p64[c->cur], c->ids[c->cur], dst, id0);
+    else
+        k_soa_to_f32<<<grid_for(n, 256), 256, 0, c->stream>>>(s, n, c->p32[c->cur], c->ids[c->cur], dst, id0, c->g.nx,
+                                                               c->g.ny, c->g.nz, c->diag);
+    ++c->launches;
+}
+
+void launch_to_host_soa(ohpic_ctx *c, const Soa6w &out, int64_t src, int64_t n)
+{
+    if (n <= 0) return;
+    if (c->cfg.precision == OHPIC_FP64)
+        k_f64_to_soa<<<grid_for(n, 256), 256, 0, c->stream>>>(c->p64[c->cur], src, n, out);
+    else
+        k_f32_to_soa<<<grid_for(n, 256), 256, 0, c->stream>>>(c->p32[c->cur], src, n, out);
     ++c->launches;
 }
 

@@ -81,6 +81,19 @@ void species_consts(const ohpic_config &cfg, int s, double dt, SpeciesConst &k)
     k.mass = k.q / k.qm;
 }
 
+// The device address of a host array the GPU can reach directly (pinned with
+// cudaHostAlloc/cudaMallocHost or registered with cudaHostRegister), else null.
+const void *device_view(const void *host)
+{
+    if (!host) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 }  // namespace ohpic
 
 namespace {
@@ -372,7 +385,16 @@ int ohpic_upload_particles_soa(ohpic_ctx *c, int s, const double *x, const doubl
     const int64_t chunk = std::max<int64_t>(1, c->stage_bytes / 48);
     double *stage = (double *)c->stage;
     const double *src[6] = {x, y, z, vx, vy, vz};
-    for (int64_t a = 0; a < n; a += chunk) {
+    // Arrays the GPU can reach (pinned or registered) are read by the conversion
+    // kernel itself; others go through the device staging buffer chunk by chunk.
+    Soa6 direct;
+    bool all_direct = n > 0;
+    for (int k = 0; k < 6 && all_direct; ++k) {
+        direct.p[k] = (const double *)device_view(src[k]);
+        all_direct = direct.p[k] != nullptr;
+    }
+    if (all_direct) launch_from_host_soa(c, direct, n, c->seg[s], 0);
+    for (int64_t a = 0; a < n && !all_direct; a += chunk) {
         const int64_t m = std::min(chunk, n - a);
         for (int k = 0; k < 6; ++k)
             OHPIC_CUDA_TRY(c, cudaMemcpyAsync(stage + k * m, src[k] + a, sizeof(double) * m, cudaMemcpyHostToDevice,
@@ -441,7 +463,21 @@ int ohpic_download_particles_soa(ohpic_ctx *c, int s, double *x, double *y, doub
     const int64_t chunk = std::max<int64_t>(1, c->stage_bytes / 48);
     double *stage = (double *)c->stage;
     double *dst[6] = {x, y, z, vx, vy, vz};
-    for (int64_t a = 0; a < n; a += chunk) {
+    // Arrays the GPU can reach (pinned or registered) are written by the
+    // conversion kernel itself; others come back through the staging buffer.
+    Soa6w direct;
+    bool all_direct = n > 0;
+    for (int k = 0; k < 6 && all_direct; ++k) {
+        direct.p[k] = dst[k] ? (double *)device_view(dst[k]) : nullptr;
+        all_direct = !dst[k] || direct.p[k] != nullptr;
+    }
+    if (all_direct) {
+        launch_to_host_soa(c, direct, c->seg[s], n);
+        if (ids)
+            OHPIC_CUDA_TRY(c, cudaMemcpyAsync(ids, c->ids[c->cur] + c->seg[s], sizeof(uint32_t) * n,
+                                              cudaMemcpyDeviceToHost, c->stream));
+    }
+    for (int64_t a = 0; a < n && !all_direct; a += chunk) {
         const int64_t m = std::min(chunk, n - a);
         launch_to_f64_stage(c, stage, c->seg[s] + a, m);
         for (int k = 0; k < 6; ++k)

@@ -295,6 +295,18 @@ void launch_f64_to_f32(ohpic_ctx *c, const double *stage6, int64_t n, int64_t ds
 void launch_f64_soa_from_stage(ohpic_ctx *c, const double *stage, int64_t n, int64_t dst, uint32_t id0,
                                int aos, int64_t stride_doubles);
 void launch_to_f64_stage(ohpic_ctx *c, double *stage, int64_t src, int64_t n);
+// Six FP64 SoA arrays the kernels read or write directly (device-accessible host
+// memory: pinned or registered); a null output array is skipped.
+struct Soa6 {
+    const double *p[6];
+};
+struct Soa6w {
+    double *p[6];
+};
+void launch_from_host_soa(ohpic_ctx *c, const Soa6 &s, int64_t n, int64_t dst, uint32_t id0);
+void launch_to_host_soa(ohpic_ctx *c, const Soa6w &out, int64_t src, int64_t n);
+// The device address of a host array the GPU can reach (pinned or registered), else null.
+const void *device_view(const void *host);
 void launch_kinetic(ohpic_ctx *c);
 // Device-side initial conditions (init.cu).
 int init_particles(ohpic_ctx *c, uint64_t initstate, uint64_t initseq, uint64_t advance,
