@@ -195,7 +195,7 @@ def timed_steps(ctx, wl, k: int, on_step=None):
 
 def tune_form(P, wl, form, args) -> dict | None:
     """Launch shape for this workload from the autotuner, measured on a proxy grid
-    of at most 128 x 128 x 64 cells with the same particles per cell and physics
+    of at most 256 x 128 x 64 cells with the same particles per cell and physics
     (the sort cadence stays the workload's)."""
     if args.tuning:
         return dict(json.loads(args.tuning), tuned_on="given on the command line")
@@ -205,8 +205,8 @@ def tune_form(P, wl, form, args) -> dict | None:
     t0 = time.perf_counter()
     t = autotune.tune(n=wl.n, dt=wl.dt, b0=wl.b0, qm=[s.qm for s in wl.species], q=[s.q for s in wl.species],
                       capacity_per_cell=[s.ppc * 1.02 + 1 for s in wl.species], species=species_inits(P, wl),
-                      precision=P.FP32 if form == "fp32" else P.FP64, weights=args.weights, steps=3,
-                      max_cadence=40)
+                      precision=P.FP32 if form == "fp32" else P.FP64, weights=args.weights, steps=4,
+                      max_cadence=40, proxy_limit=(256, 128, 64))
     keep = ("tile", "halo", "split", "deposit", "lane_particles")
     return {**{k: t[k] for k in keep}, "sort_every_suggested": t["sort_every"],
             "tuned_on": list(t["grid_tuned_on"]), "trials": len(t["trials"]),

@@ -1,16 +1,17 @@
 """Autotuner for the launch shape of the particle kernels.
 
 Picks, per grid size and plasma, the tile shape, the halo staged around a tile,
-the CTAs per (species, tile), the FP32 warp-deposit reduction and the cell-sort
-cadence.  It measures on a throwaway context filled by the device injector with
+the CTAs per (species, tile), the FP32 particles per lane and warp-deposit
+reduction, and the cell-sort cadence.  It measures on a throwaway context filled by the device injector with
 the same particles per cell and physics as the run, so tuning never advances the
 caller's simulation.  The per-CTA work depends only on the tile and the plasma,
 not on the grid size, so large grids are tuned on a proxy grid (by default at
 most 128 x 128 x 64 cells) holding the same particles per cell; CTAs per tile
 only matter when the grid has few tiles, where the proxy is the grid itself.
 
-Search: coordinate descent from the library defaults -- deposit reduction, then
-tile shape, halo, split -- each candidate timed as the mean fused-push time over
+Search: coordinate descent from the library defaults -- particles per lane,
+deposit reduction, halo, tile shape, halo again, split -- each candidate timed
+as the mean fused-push time over
 a few steps right after a sort; then the sort cadence K minimising
 (sort time + sum of push times over K steps) / K.
 """
@@ -74,12 +75,14 @@ def _sort_ms(ctx: PicContext) -> float:
 
 
 def tune(n, dt, b0, qm, q, capacity_per_cell, species, precision=FP32, weights=0, proxy=True,
-         steps=3, max_cadence=40, log=None) -> dict:
+         steps=3, max_cadence=40, log=None, proxy_limit=(128, 128, 64)) -> dict:
     """Returns the best tuning dict for a run on grid n.
 
     species: list of SpeciesInit (device injector parameters) of the run;
-    capacity_per_cell: particles per cell to reserve per species (>= ppc)."""
-    grid = proxy_grid(n) if proxy else tuple(n)
+    capacity_per_cell: particles per cell to reserve per species (>= ppc);
+    proxy_limit: the largest proxy grid.  A proxy with many tiles per SM ranks
+    tile shapes as the full grid does; a small one favours small tiles."""
+    grid = proxy_grid(n, proxy_limit) if proxy else tuple(n)
     ncell = grid[0] * grid[1] * grid[2]
     caps = [int(c * ncell) + 1024 for c in capacity_per_cell]
     cfg_kw = dict(n=grid, dt=dt, b0=b0, qm=qm, q=q, capacity=caps, precision=precision, weights=weights,
@@ -116,6 +119,8 @@ def tune(n, dt, b0, qm, q, capacity_per_cell, species, precision=FP32, weights=0
         if precision == FP32:
             descend("lane_particles", [2, 4])
             descend("deposit", [DEPOSIT_RUNS, DEPOSIT_GROUPS, DEPOSIT_UNIFORM, DEPOSIT_MATCH])
+        # halo first: it sets the shared memory per CTA and so which tiles keep two CTAs per SM
+        descend("halo", [1, 2, 3])
         descend("tile", _tiles(grid))
         descend("halo", [1, 2, 3])
         if not proxy or grid == tuple(n):
