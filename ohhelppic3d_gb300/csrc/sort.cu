@@ -2,7 +2,7 @@
 //
 // No reference counterpart: the reference walks an unsorted oh_particle buffer.
 // The sort makes the particles of one tile a contiguous range so the fused push
-// can stage that tile's fields in shared memory (particles.cu).
+// can stage that tile's fields in shared memory (push_f32.cu, push_f64.cu).
 //
 // Per species: histogram of cell keys (global atomics, aggregated per warp with
 // __match_any_sync), exclusive scan of the ncell counters (multi-level block
