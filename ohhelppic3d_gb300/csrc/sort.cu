@@ -63,39 +63,107 @@ __device__ __forceinline__ uint32_t aggregated_inc(uint32_t *count, uint32_t key
     return base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
 }
 
+// The sort kernels are bound by memory latency (a cell load, then an atomic, then
+// the record), so each thread keeps several independent particles in flight:
+// four per iteration in the histogram, two in the scatter, whose record loads are
+// all issued before the atomics.
 template <bool F32>
 __global__ void k_hist(Geom g, PartF64 p64, PartF32 p32, int64_t seg, int64_t n, uint32_t *count, DevDiag *d)
 {
+    constexpr int U = 4;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += stride) {
-        const int64_t i = base + threadIdx.x;
-        const bool active = i < n;
-        const uint32_t key = active ? particle_key<F32>(g, p64, p32, seg + i, d) : 0u;
-        aggregated_inc(count, key, active);
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += U * stride) {
+        uint32_t key[U];
+        bool act[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t i = base + u * stride + threadIdx.x;
+            act[u] = i < n;
+            key[u] = act[u] ? particle_key<F32>(g, p64, p32, seg + i, d) : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) aggregated_inc(count, key[u], act[u]);
     }
+}
+
+// One particle's record in registers.
+template <bool F32>
+struct Rec {
+    double a[6];      // FP64 form: x, y, z, vx, vy, vz
+    int32_t cell;     // FP32 form: packed cell, then offsets and velocities in f[]
+    float f[6];
+    uint32_t id;
+};
+
+template <bool F32>
+__device__ __forceinline__ void rec_load(const PartF64 &s64, const PartF32 &s32, const uint32_t *sid, int64_t i,
+                                         Rec<F32> &r)
+{
+    if (F32) {
+        r.cell = s32.cell[i];
+        r.f[0] = s32.ox[i]; r.f[1] = s32.oy[i]; r.f[2] = s32.oz[i];
+        r.f[3] = s32.vx[i]; r.f[4] = s32.vy[i]; r.f[5] = s32.vz[i];
+    } else {
+        r.a[0] = s64.x[i]; r.a[1] = s64.y[i]; r.a[2] = s64.z[i];
+        r.a[3] = s64.vx[i]; r.a[4] = s64.vy[i]; r.a[5] = s64.vz[i];
+    }
+    r.id = sid ? sid[i] : 0u;
+}
+
+template <bool F32>
+__device__ __forceinline__ void rec_store(const PartF64 &d64, const PartF32 &d32, uint32_t *did, int64_t j,
+                                          const Rec<F32> &r)
+{
+    if (F32) {
+        d32.cell[j] = r.cell;
+        d32.ox[j] = r.f[0]; d32.oy[j] = r.f[1]; d32.oz[j] = r.f[2];
+        d32.vx[j] = r.f[3]; d32.vy[j] = r.f[4]; d32.vz[j] = r.f[5];
+    } else {
+        d64.x[j] = r.a[0]; d64.y[j] = r.a[1]; d64.z[j] = r.a[2];
+        d64.vx[j] = r.a[3]; d64.vy[j] = r.a[4]; d64.vz[j] = r.a[5];
+    }
+    if (did) did[j] = r.id;
+}
+
+template <bool F32>
+__device__ __forceinline__ uint32_t rec_key(const Geom &g, const Rec<F32> &r, DevDiag *d)
+{
+    int ix, iy, iz;
+    if (F32) {
+        ix = cell_x(r.cell); iy = cell_y(r.cell); iz = cell_z(r.cell);
+    } else {
+        ix = (int)r.a[0]; iy = (int)r.a[1]; iz = (int)r.a[2];
+    }
+    if ((unsigned)ix >= (unsigned)g.nx || (unsigned)iy >= (unsigned)g.ny || (unsigned)iz >= (unsigned)g.nz) {
+        if (atomicCAS(&d->err_code, 0, OHPIC_ERR_BOUNDS) == 0) d->err_info = 10;
+        ix = iy = iz = 0;
+    }
+    return tile_key(g, ix, iy, iz);
 }
 
 template <bool F32>
 __global__ void k_scatter(Geom g, PartF64 s64, PartF32 s32, PartF64 d64, PartF32 d32, const uint32_t *sid,
                           uint32_t *did, int64_t seg, int64_t n, const uint32_t *start, uint32_t *cursor, DevDiag *d)
 {
+    constexpr int U = 2;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += stride) {
-        const int64_t i = base + threadIdx.x;
-        const bool active = i < n;
-        const uint32_t key = active ? particle_key<F32>(g, s64, s32, seg + i, d) : 0u;
-        const uint32_t slot = aggregated_inc(cursor, key, active);
-        if (!active) continue;
-        const int64_t src = seg + i, dst = seg + (int64_t)start[key] + slot;
-        if (F32) {
-            d32.cell[dst] = s32.cell[src];
-            d32.ox[dst] = s32.ox[src]; d32.oy[dst] = s32.oy[src]; d32.oz[dst] = s32.oz[src];
-            d32.vx[dst] = s32.vx[src]; d32.vy[dst] = s32.vy[src]; d32.vz[dst] = s32.vz[src];
-        } else {
-            d64.x[dst] = s64.x[src]; d64.y[dst] = s64.y[src]; d64.z[dst] = s64.z[src];
-            d64.vx[dst] = s64.vx[src]; d64.vy[dst] = s64.vy[src]; d64.vz[dst] = s64.vz[src];
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += U * stride) {
+        Rec<F32> r[U];
+        bool act[U];
+        uint32_t key[U], slot[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t i = base + u * stride + threadIdx.x;
+            act[u] = i < n;
+            if (act[u]) rec_load<F32>(s64, s32, sid, seg + i, r[u]);
         }
-        if (sid) did[dst] = sid[src];
+#pragma unroll
+        for (int u = 0; u < U; ++u) key[u] = act[u] ? rec_key<F32>(g, r[u], d) : 0u;
+#pragma unroll
+        for (int u = 0; u < U; ++u) slot[u] = aggregated_inc(cursor, key[u], act[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (act[u]) rec_store<F32>(d64, d32, did, seg + (int64_t)start[key[u]] + slot[u], r[u]);
     }
 }
 
