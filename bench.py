@@ -5,7 +5,8 @@ particles), run in the FP32 precision form (headline `value`) and the plain
 FP64 form (`fp64_form`).  A step is one mainstep: spectral field solve, then
 the fused gather + Boris + periodic wrap + deposit over every particle; the
 cell sort runs every 20 steps counted from the first timed step (so a timed
-region of K <= 20 steps always contains one sort).
+region of K <= 20 steps always contains one sort), and the warm-up runs whole
+sort cycles, so the timed sort follows a full cycle of particle drift.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--workload c2|c1|c4] [--forms fp32,fp64] [--no-e2e] [--no-cpu-baseline]
@@ -195,8 +196,9 @@ def timed_steps(ctx, wl, k: int, on_step=None):
 
 def tune_form(P, wl, form, args) -> dict | None:
     """Launch shape for this workload from the autotuner, measured on a proxy grid
-    of at most 256 x 128 x 64 cells with the same particles per cell and physics
-    (the sort cadence stays the workload's)."""
+    of at most 256 x 128 x 64 cells with the same particles per cell and physics,
+    each candidate ranked by its mean push over one sort cycle (the sort cadence
+    stays the workload's)."""
     if args.tuning:
         return dict(json.loads(args.tuning), tuned_on="given on the command line")
     if args.no_tune:
@@ -205,7 +207,8 @@ def tune_form(P, wl, form, args) -> dict | None:
     t0 = time.perf_counter()
     t = autotune.tune(n=wl.n, dt=wl.dt, b0=wl.b0, qm=[s.qm for s in wl.species], q=[s.q for s in wl.species],
                       capacity_per_cell=[s.ppc * 1.02 + 1 for s in wl.species], species=species_inits(P, wl),
-                      precision=P.FP32 if form == "fp32" else P.FP64, weights=args.weights, steps=4,
+                      precision=P.FP32 if form == "fp32" else P.FP64, weights=args.weights,
+                      steps=max(4, wl.sort_every - 1),
                       max_cadence=40, proxy_limit=(256, 128, 64))
     keep = ("tile", "halo", "split", "deposit", "lane_particles")
     return {**{k: t[k] for k in keep}, "sort_every_suggested": t["sort_every"],
@@ -221,9 +224,13 @@ def run_form(P, torch, dist, wl, form, args, sampler, peak):
         autotune.apply(ctx, tuning, keep_sort_every=True)
     counts = ctx.init_particles(species_inits(P, wl), seed=(42, 52 + dist.rank))
     n_local = sum(counts)
-    ctx.sort()
-    for _ in range(args.warmup):
-        ctx.step(wl.dt, 1)
+    # warm-up in whole sort cycles (at least --warmup steps), so that the timed
+    # region's first sort meets particles that drifted for a full cycle, as every
+    # sort of a long run does
+    warm = -(-args.warmup // wl.sort_every) * wl.sort_every if wl.sort_every else args.warmup
+    if not wl.sort_every:
+        ctx.sort()
+    timed_steps(ctx, wl, warm)
     ctx.synchronize()
     ctx.set_push_timing(True)
     launches0 = ctx.stats()["launches"]
@@ -260,6 +267,7 @@ def run_form(P, torch, dist, wl, form, args, sampler, peak):
         "gpu_launches": st["launches"] - launches0,
         "tuning": dict(tuning or {}, applied=ctx.get_tuning()),
         "sort_every": wl.sort_every,
+        "warmup_steps_run": warm,
     }
     return ctx, counts, out
 
@@ -524,6 +532,7 @@ def main(argv=None) -> int:
         "config": {"workload": wl.description, "form": {"fp32": "FP32 precision form (int32 cell + FP32 offset)",
                                                         "fp64": "plain FP64 form"}[head],
                    "weights": _wname(args.weights), "particles": r["particles"], "sort_every": r["sort_every"],
+                   "warmup_steps_run": r["warmup_steps_run"],
                    "l2": (f"inputs larger than L2: {r['particles'] * (28 if head == 'fp32' else 48) / 1e9:.1f} GB "
                           f"of particle state per GPU against a 129 MB L2"),
                    "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU"},

@@ -11,9 +11,10 @@ only matter when the grid has few tiles, where the proxy is the grid itself.
 
 Search: coordinate descent from the library defaults -- particles per lane,
 deposit reduction, halo, tile shape, halo again, split -- each candidate timed
-as the mean fused-push time over
-a few steps right after a sort; then the sort cadence K minimising
-(sort time + sum of push times over K steps) / K.
+as the mean fused-push time over `steps` steps after a sort (a whole sort cycle
+ranks the shapes as a long run sees them: particles drift out of their tiles
+between sorts, which favours larger halos late in the cycle); then the sort
+cadence K minimising (sort time + sum of push times over K steps) / K.
 """
 from __future__ import annotations
 

@@ -197,6 +197,9 @@ struct ohpic_ctx {
     ohpic::PartF64 p64[2];
     ohpic::PartF32 p32[2];
     uint32_t *ids[2];
+    // FP32 form: each buffer is one allocation of eight word arrays (cell, offsets,
+    // velocities, ids), so it also holds N 32-byte sort records.
+    void *p32_block[2];
     int cur;
 
     // fields

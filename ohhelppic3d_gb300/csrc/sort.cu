@@ -6,10 +6,11 @@
 //
 // Per species: histogram of cell keys (global atomics, aggregated per warp with
 // __match_any_sync), exclusive scan of the ncell counters (multi-level block
-// scan), tile start table, then a scatter of every particle array into the
-// second buffer.  Lanes of a warp that share a key take consecutive slots in
-// lane order, so a warp's relative order is kept; order across warps follows
-// the atomic order.
+// scan), tile start table, then a scatter of every particle into the second
+// buffer (FP32 form: as 32-byte records, transposed back into the first buffer's
+// word arrays by a sequential pass).  Lanes of a warp that share a key take
+// consecutive slots in lane order, so a warp's relative order is kept; order
+// across warps follows the atomic order.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -164,6 +165,58 @@ __global__ void k_scatter(Geom g, PartF64 s64, PartF32 s32, PartF64 d64, PartF32
 #pragma unroll
         for (int u = 0; u < U; ++u)
             if (act[u]) rec_store<F32>(d64, d32, did, seg + (int64_t)start[key[u]] + slot[u], r[u]);
+    }
+}
+
+// FP32 form: the scatter writes each particle as one 32-byte record (cell, three
+// offsets, three velocities, id) -- a whole L2 sector.  Once particles have
+// drifted across tiles, a destination cell's slots are filled from source ranges
+// megabytes apart, so per-array 4-byte scatters would leave sectors partly
+// written when L2 evicts them (each costing a read-modify-write of the sector in
+// HBM); whole-sector records never do.  A sequential pass then transposes the
+// records back into the word arrays.
+__device__ __forceinline__ void rec32_store(int4 *rec, int64_t j, const Rec<true> &r)
+{
+    rec[2 * j] = make_int4(r.cell, __float_as_int(r.f[0]), __float_as_int(r.f[1]), __float_as_int(r.f[2]));
+    rec[2 * j + 1] = make_int4(__float_as_int(r.f[3]), __float_as_int(r.f[4]), __float_as_int(r.f[5]), (int)r.id);
+}
+
+__global__ void k_scatter_rec32(Geom g, PartF32 s32, const uint32_t *sid, int4 *rec, int64_t seg, int64_t n,
+                                const uint32_t *start, uint32_t *cursor, DevDiag *d)
+{
+    constexpr int U = 2;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += U * stride) {
+        Rec<true> r[U];
+        bool act[U];
+        uint32_t key[U], slot[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t i = base + u * stride + threadIdx.x;
+            act[u] = i < n;
+            if (act[u]) rec_load<true>(PartF64{}, s32, sid, seg + i, r[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) key[u] = act[u] ? rec_key<true>(g, r[u], d) : 0u;
+#pragma unroll
+        for (int u = 0; u < U; ++u) slot[u] = aggregated_inc(cursor, key[u], act[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (act[u]) rec32_store(rec, seg + (int64_t)start[key[u]] + slot[u], r[u]);
+    }
+}
+
+// Records [seg, seg + n) back into the word arrays (ids only when tracked).
+__global__ void k_rec32_to_soa(const int4 *rec, int64_t seg, int64_t n, PartF32 p, uint32_t *ids)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int64_t j = seg + i;
+        const int4 a = rec[2 * j], b = rec[2 * j + 1];
+        p.cell[j] = a.x;
+        p.ox[j] = __int_as_float(a.y); p.oy[j] = __int_as_float(a.z); p.oz[j] = __int_as_float(a.w);
+        p.vx[j] = __int_as_float(b.x); p.vy[j] = __int_as_float(b.y); p.vz[j] = __int_as_float(b.z);
+        if (ids) ids[j] = (uint32_t)b.w;
     }
 }
 
@@ -399,18 +452,22 @@ int sort_particles(ohpic_ctx *c)
         ++c->launches;
         if (n > 0) {
             cudaMemsetAsync(c->cell_count, 0, sizeof(uint32_t) * g.ncell, c->stream);
-            if (f32)
-                k_scatter<true><<<grid_of(n), 256, 0, c->stream>>>(g, c->p64[src], c->p32[src], c->p64[dst],
-                                                                   c->p32[dst], c->ids[src], c->ids[dst], c->seg[s],
-                                                                   n, c->cell_start, c->cell_count, c->diag);
-            else
+            if (f32) {
+                // records in the other buffer's block, then back into this buffer
+                int4 *rec = (int4 *)c->p32_block[dst];
+                k_scatter_rec32<<<grid_of(n), 256, 0, c->stream>>>(g, c->p32[src], c->ids[src], rec, c->seg[s], n,
+                                                                   c->cell_start, c->cell_count, c->diag);
+                k_rec32_to_soa<<<grid_of(n), 256, 0, c->stream>>>(rec, c->seg[s], n, c->p32[src], c->ids[src]);
+                c->launches += 2;
+            } else {
                 k_scatter<false><<<grid_of(n), 256, 0, c->stream>>>(g, c->p64[src], c->p32[src], c->p64[dst],
                                                                     c->p32[dst], c->ids[src], c->ids[dst], c->seg[s],
                                                                     n, c->cell_start, c->cell_count, c->diag);
-            ++c->launches;
+                ++c->launches;
+            }
         }
     }
-    c->cur = dst;
+    if (!f32) c->cur = dst;   // the FP32 records come back into the same buffer
     c->sorted = true;
     c->steps_since_sort = 0;
     return OHPIC_OK;
