@@ -208,7 +208,7 @@ def tune_form(P, wl, form, args) -> dict | None:
     t = autotune.tune(n=wl.n, dt=wl.dt, b0=wl.b0, qm=[s.qm for s in wl.species], q=[s.q for s in wl.species],
                       capacity_per_cell=[s.ppc * 1.02 + 1 for s in wl.species], species=species_inits(P, wl),
                       precision=P.FP32 if form == "fp32" else P.FP64, weights=args.weights,
-                      steps=max(4, wl.sort_every - 1),
+                      steps=max(4, wl.sort_every - 1) if form == "fp32" else 4,
                       max_cadence=40, proxy_limit=(256, 128, 64))
     keep = ("tile", "halo", "split", "deposit", "lane_particles")
     return {**{k: t[k] for k in keep}, "sort_every_suggested": t["sort_every"],

@@ -9,8 +9,8 @@ not on the grid size, so large grids are tuned on a proxy grid (by default at
 most 128 x 128 x 64 cells) holding the same particles per cell; CTAs per tile
 only matter when the grid has few tiles, where the proxy is the grid itself.
 
-Search: coordinate descent from the library defaults -- particles per lane,
-deposit reduction, halo, tile shape, halo again, split -- each candidate timed
+Search: from the library defaults, particles per lane, deposit reduction,
+every (tile shape, halo) pair, particles per lane again, split -- each candidate timed
 as the mean fused-push time over `steps` steps after a sort (a whole sort cycle
 ranks the shapes as a long run sees them: particles drift out of their tiles
 between sorts, which favours larger halos late in the cycle); then the sort
@@ -103,27 +103,33 @@ def tune(n, dt, b0, qm, q, capacity_per_cell, species, precision=FP32, weights=0
             log(f"tune {grid} {kw} -> {ms:.3f} ms")
         return ms
 
-    def descend(key, values):
+    def joint(candidates):
+        """Measures every candidate (a dict of tuning keys) on top of the current best."""
         nonlocal best
         base = dict(best)
-        scores = {}
-        for v in values:
-            s = measure(**{**base, key: v})
+        scores = []
+        for cand in candidates:
+            s = measure(**{**base, **cand})
             if s is not None:
-                scores[v] = s
+                scores.append((s, cand))
         if scores:
-            pick = min(scores, key=scores.get)
-            best = {**base, key: pick}
+            best = {**base, **min(scores, key=lambda x: x[0])[1]}
             ctx.set_tuning(**best)
+
+    def descend(key, values):
+        joint([{key: v} for v in values])
 
     try:
         if precision == FP32:
             descend("lane_particles", [2, 4])
             descend("deposit", [DEPOSIT_RUNS, DEPOSIT_GROUPS, DEPOSIT_UNIFORM, DEPOSIT_MATCH])
-        # halo first: it sets the shared memory per CTA and so which tiles keep two CTAs per SM
-        descend("halo", [1, 2, 3])
-        descend("tile", _tiles(grid))
-        descend("halo", [1, 2, 3])
+        # tile and halo together: the halo's absolute width sets how far particles
+        # drift before they leave the staged box, and with the tile it sets the
+        # shared memory per CTA, so a small tile with a wide halo can beat both a
+        # wide halo alone and a large tile alone
+        joint([{"tile": t, "halo": h} for t in _tiles(grid) for h in (1, 2, 3)])
+        if precision == FP32:
+            descend("lane_particles", [2, 4])
         if not proxy or grid == tuple(n):
             descend("split", [1, 2, 4, 8])
         # sort cadence: per-step push time grows as particles drift out of their tiles

@@ -22,12 +22,12 @@ def test_proxy_grid_and_candidate_tiles():
         assert tiles and all(n[d] % t[d] == 0 for t in tiles for d in range(3))
 
 
-def _run(P, tuning: dict, steps: int = 6):
+def _run(P, tuning: dict, steps: int = 6, vth: float = 1.4):
     n = (32, 32, 16)
     ppc = 8
     qm = [-1.0, 0.01]
     q = [1.0 / qm[0] / ppc, 0.01 / qm[1] / ppc]
-    sp = [P.species_init(ppc, 1.4), P.species_init(ppc, 0.14)]
+    sp = [P.species_init(ppc, vth), P.species_init(ppc, 0.1 * vth)]
     cap = [2 * ppc * n[0] * n[1] * n[2]] * 2
     cfg = P.make_config(n=n, dt=0.1, b0=(0.0, 0.0, 0.6), qm=qm, q=q, capacity=cap, precision=P.FP32, sort_every=10)
     with P.PicContext(cfg) as ctx:
@@ -53,6 +53,29 @@ def test_fp32_state_identical_across_launch_shapes(ohpic):
                 {"lane_particles": 2, "split": 2, "halo": 1}, {"lane_particles": 2, "sort_every": 1}]
     for v in variants:
         f, p, d = _run(P, v)
+        for w in f:
+            assert np.array_equal(f[w], ref_f[w]), (v, w)
+        for s in range(2):
+            for k in ("x", "y", "z", "vx", "vy", "vz"):
+                assert np.array_equal(p[s][k], ref_p[s][k]), (v, s, k)
+        assert d["crossings"] == ref_d["crossings"], v
+
+
+@pytest.mark.gpu
+def test_fp32_particles_outside_their_box_identical(ohpic):
+    """Without a re-sort, fast particles drift far outside their tile's staged box.
+    The four-per-lane pass queues those per warp and runs them 32 at a time; its
+    state must match the two-per-lane pass (every particle inline) and a run that
+    re-sorts before every step (no particle outside its box)."""
+    P = ohpic
+    base = {"tile": (8, 8, 8), "halo": 1}
+    ref_f, ref_p, ref_d = _run(P, dict(base, sort_every=1), steps=24, vth=4.0)
+    for v in (dict(base, sort_every=1000, lane_particles=4), dict(base, sort_every=1000, lane_particles=2),
+              dict(base, sort_every=1000, lane_particles=4, deposit=P.DEPOSIT_MATCH)):
+        f, p, d = _run(P, v, steps=24, vth=4.0)
+        # the queue was exercised (a sorted run has only the few particles of the
+        # four-particle groups that straddle a tile boundary outside)
+        assert d["outside_tile"] > 1000 + 10 * ref_d["outside_tile"], (v, d["outside_tile"])
         for w in f:
             assert np.array_equal(f[w], ref_f[w]), (v, w)
         for s in range(2):
