@@ -142,9 +142,9 @@ struct MultiPush {
 // all segments, so one exclusive scan serves every run.
 struct SortSeg {
     Geom g;
-    PartF32 src, dst;
-    const uint32_t *ids_src;
-    uint32_t *ids_dst;
+    PartF32 p;               // sorted in place, through the record area
+    uint32_t *ids;           // may be null
+    int4 *rec;               // the run's record area: 32 bytes per particle slot
     int64_t off, count;      // particles [off, off + count) of the run's arrays
     int64_t key_base;
     int64_t *tile_begin;     // ntile + 1 entries, absolute particle indices

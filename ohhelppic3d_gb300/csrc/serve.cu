@@ -150,9 +150,9 @@ struct Run {
     int64_t bytes = 0;            // device bytes held from admission to release
     int64_t out_doubles = 0;      // kept fields + particles
     void *mem = nullptr;
-    PartF32 p[2]{};
-    uint32_t *ids[2] = {nullptr, nullptr};
-    int cur = 0;
+    PartF32 p{};                  // the particles, sorted in place
+    uint32_t *ids = nullptr;      // with keep_particles
+    int4 *rec = nullptr;          // sort record area, 32 bytes per slot
     int64_t *tile_begin = nullptr;
     DevDiag *diag = nullptr;
     double *out = nullptr;
@@ -172,7 +172,7 @@ struct Run {
 
 // Byte layout of a run's single allocation.
 struct RunLayout {
-    int64_t p0, p1, ids0, ids1, tile_begin, diag, out, total;
+    int64_t p, ids, rec, tile_begin, diag, out, total;
 };
 
 RunLayout run_layout(int64_t slots, int nsp, int64_t ntile, bool ids, int64_t out_doubles)
@@ -180,10 +180,9 @@ RunLayout run_layout(int64_t slots, int nsp, int64_t ntile, bool ids, int64_t ou
     RunLayout L{};
     int64_t off = 0;
     const int64_t part = align256(slots * 4);
-    L.p0 = off; off += 7 * part;
-    L.p1 = off; off += 7 * part;
-    L.ids0 = off; off += ids ? part : 0;
-    L.ids1 = off; off += ids ? part : 0;
+    L.p = off; off += 7 * part;
+    L.ids = off; off += ids ? part : 0;
+    L.rec = off; off += align256(slots * 32);
     L.tile_begin = off; off += align256((int64_t)nsp * (ntile + 1) * 8);
     L.diag = off; off += align256((int64_t)sizeof(DevDiag));
     L.out = off; off += align256(out_doubles * 8);
@@ -263,7 +262,6 @@ struct ohpic_server {
     cudaEvent_t tick_ev[kDepth] = {};
     int64_t ticks = 0;
     int ticks_since_sort = 0;
-    bool last_was_sort = false;
     // shapes of the uploaded tables
     int tab_nruns = 0, tab_nseg = 0;
     int64_t tab_items = 0, tab_chunks = 0, tab_max_ntile = 0, tab_particles = 0;
@@ -417,8 +415,8 @@ void destroy_pool(Server *s, Pool *P)
         sfree(s, p);
 }
 
-// Run descriptor for the multi-run push; pc = the particle buffer it reads.
-RunDesc make_desc(const Server *s, const Run *r, int pc)
+// Run descriptor for the multi-run push.
+RunDesc make_desc(const Server *s, const Run *r)
 {
     RunDesc d;
     memset(&d, 0, sizeof(d));
@@ -446,7 +444,7 @@ RunDesc make_desc(const Server *s, const Run *r, int pc)
     a.interp_out = nullptr;
     a.diag = r->diag;
     a.chunk = 4096;
-    d.p = r->p[pc];
+    d.p = r->p;
     return d;
 }
 
@@ -466,9 +464,8 @@ void stage_done(Server *s, int slot)
 }
 
 // Uploads the tables of `runs` (in queue order: decreasing particles per item)
-// and the slot masks of every pool.  post_sort: the push reads the buffer the
-// sort of this tick writes.  Sets the launch shapes.
-bool upload_tables(Server *s, std::vector<Run *> &runs, bool post_sort)
+// and the slot masks of every pool.  Sets the launch shapes.
+bool upload_tables(Server *s, std::vector<Run *> &runs)
 {
     std::stable_sort(runs.begin(), runs.end(), [](const Run *x, const Run *y) {
         return (double)x->total / (double)std::max<int64_t>(x->items, 1) >
@@ -497,8 +494,7 @@ bool upload_tables(Server *s, std::vector<Run *> &runs, bool post_sort)
     int si = 0;
     for (int i = 0; i < n; ++i) {
         Run *r = runs[i];
-        const int pc = post_sort ? 1 - r->cur : r->cur;
-        hr[i] = make_desc(s, r, pc);
+        hr[i] = make_desc(s, r);
         items += r->items;
         he[i] = items;
         parts += r->total;
@@ -508,10 +504,9 @@ bool upload_tables(Server *s, std::vector<Run *> &runs, bool post_sort)
             SortSeg &sg = hs[si];
             memset(&sg, 0, sizeof(sg));
             sg.g = r->g;
-            sg.src = r->p[r->cur];
-            sg.dst = r->p[1 - r->cur];
-            sg.ids_src = r->ids[r->cur];
-            sg.ids_dst = r->ids[1 - r->cur];
+            sg.p = r->p;
+            sg.ids = r->ids;
+            sg.rec = r->rec;
             sg.off = r->seg[k];
             sg.count = r->count[k];
             sg.key_base = P.key_base + ((int64_t)r->slot * P.f.nsp + k) * r->g.ncell;
@@ -664,7 +659,7 @@ void retire_enqueue(Server *s, Run *r)
     cudaMemsetAsync(r->diag->kin, 0, sizeof(r->diag->kin), s->st);
     for (int k = 0; k < r->nsp; ++k)
         if (r->count[k] > 0)
-            k_run_kinetic<<<grid_for(r->count[k]), 256, 0, s->st>>>(r->p[r->cur], r->seg[k], r->count[k],
+            k_run_kinetic<<<grid_for(r->count[k]), 256, 0, s->st>>>(r->p, r->seg[k], r->count[k],
                                                                     &r->diag->kin[k][0]);
     int64_t off = 0;
     if (r->req.keep_fields) {
@@ -674,7 +669,7 @@ void retire_enqueue(Server *s, Run *r)
     if (r->req.keep_particles) {
         for (int k = 0; k < r->nsp; ++k) {
             if (r->count[k] > 0)
-                k_run_by_id<<<grid_for(r->count[k]), 256, 0, s->st>>>(r->p[r->cur], r->ids[r->cur], r->seg[k],
+                k_run_by_id<<<grid_for(r->count[k]), 256, 0, s->st>>>(r->p, r->ids, r->seg[k],
                                                                       r->count[k], r->out + off);
             off += 6 * r->count[k];
         }
@@ -787,10 +782,9 @@ bool admit(Server *s)
         unsigned char *base = (unsigned char *)r->mem;
         const bool ids = r->req.keep_particles != 0;
         const RunLayout L = run_layout(r->slots, r->nsp, r->g.ntile, ids, r->out_doubles);
-        r->p[0] = part_view(base + L.p0, r->slots);
-        r->p[1] = part_view(base + L.p1, r->slots);
-        r->ids[0] = ids ? (uint32_t *)(base + L.ids0) : nullptr;
-        r->ids[1] = ids ? (uint32_t *)(base + L.ids1) : nullptr;
+        r->p = part_view(base + L.p, r->slots);
+        r->ids = ids ? (uint32_t *)(base + L.ids) : nullptr;
+        r->rec = (int4 *)(base + L.rec);
         r->tile_begin = (int64_t *)(base + L.tile_begin);
         r->diag = (DevDiag *)(base + L.diag);
         r->out = (double *)(base + L.out);
@@ -817,11 +811,10 @@ bool admit(Server *s)
         d.spi = r->req.species;
         d.seg = r->seg;
         d.cap = nullptr;
-        d.p32 = r->p[0];
-        d.ids = r->ids[0];
+        d.p32 = r->p;
+        d.ids = r->ids;
         int64_t cnt[OHPIC_MAX_SPECIES] = {0};
         draw_particles(d, cnt, nullptr);
-        r->cur = 0;
         r->steps = 0;
         {
             std::lock_guard<std::mutex> lk(s->mu);
@@ -835,14 +828,11 @@ bool admit(Server *s)
     if (fresh.empty()) return true;
     // Sort, then deposit, the admitted runs only (the push of the next tick needs
     // their weight sums); the tick tables are rebuilt afterwards.
-    if (!upload_tables(s, fresh, true)) return false;
+    if (!upload_tables(s, fresh)) return false;
     const int64_t l = enqueue_sort(s);
     const int64_t l2 = enqueue_step(s, MODE_DEPOSIT);
     if (l2 < 0) return false;
-    for (Run *r : fresh) {
-        r->cur = 1 - r->cur;
-        s->active.push_back(r);
-    }
+    for (Run *r : fresh) s->active.push_back(r);
     s->shapes_dirty = true;
     std::lock_guard<std::mutex> lk(s->mu);
     s->stats.launches += l + l2;
@@ -883,8 +873,9 @@ bool tick(Server *s)
     const int idx = (int)(s->ticks % kDepth);
     if (s->ticks >= kDepth) cudaEventSynchronize(s->tick_ev[idx]);
     const bool sort_now = s->cfg.sort_every > 0 && s->ticks_since_sort >= s->cfg.sort_every;
-    if (s->shapes_dirty || sort_now || s->last_was_sort) {
-        if (!upload_tables(s, s->active, sort_now)) return false;
+    // the sort works in place, so the tables change only with the set of runs
+    if (s->shapes_dirty) {
+        if (!upload_tables(s, s->active)) return false;
     }
     int64_t launched = 0;
     bool via_graph = false;
@@ -920,11 +911,7 @@ bool tick(Server *s)
         launched += l;
     }
     s->shapes_dirty = false;
-    if (sort_now) {
-        for (Run *r : s->active) r->cur = 1 - r->cur;
-        s->ticks_since_sort = 0;
-    }
-    s->last_was_sort = sort_now;
+    if (sort_now) s->ticks_since_sort = 0;
     s->ticks_since_sort += 1;
     cudaEventRecord(s->tick_ev[idx], s->st);
     s->ticks += 1;

@@ -330,12 +330,14 @@ __global__ void k_hist_multi(MultiSort m)
         for (int64_t base = first; base < last; base += blockDim.x) {
             const int64_t i = base + threadIdx.x;
             const bool active = i < last;
-            const uint32_t key = active ? particle_key<true>(sg.g, PartF64{}, sg.src, sg.off + i, sg.diag) : 0u;
+            const uint32_t key = active ? particle_key<true>(sg.g, PartF64{}, sg.p, sg.off + i, sg.diag) : 0u;
             aggregated_inc(m.count + sg.key_base, key, active);
         }
     }
 }
 
+// Scatter of every segment into its run's record area (whole 32-byte records,
+// as in the single-context FP32 sort), then the records back into the arrays.
 __global__ void k_scatter_multi(MultiSort m)
 {
     __shared__ int32_t s_end[kMaxSortSegs];
@@ -350,15 +352,32 @@ __global__ void k_scatter_multi(MultiSort m)
         for (int64_t base = first; base < last; base += blockDim.x) {
             const int64_t i = base + threadIdx.x;
             const bool active = i < last;
-            const uint32_t key = active ? particle_key<true>(sg.g, PartF64{}, sg.src, sg.off + i, sg.diag) : 0u;
+            Rec<true> r;
+            if (active) rec_load<true>(PartF64{}, sg.p, sg.ids, sg.off + i, r);
+            const uint32_t key = active ? rec_key<true>(sg.g, r, sg.diag) : 0u;
             const uint32_t slot = aggregated_inc(m.cursor + sg.key_base, key, active);
-            if (!active) continue;
-            const int64_t src = sg.off + i;
-            const int64_t dst = sg.off + (int64_t)(m.start[sg.key_base + key] - base0) + slot;
-            sg.dst.cell[dst] = sg.src.cell[src];
-            sg.dst.ox[dst] = sg.src.ox[src]; sg.dst.oy[dst] = sg.src.oy[src]; sg.dst.oz[dst] = sg.src.oz[src];
-            sg.dst.vx[dst] = sg.src.vx[src]; sg.dst.vy[dst] = sg.src.vy[src]; sg.dst.vz[dst] = sg.src.vz[src];
-            if (sg.ids_src) sg.ids_dst[dst] = sg.ids_src[src];
+            if (active) rec32_store(sg.rec, sg.off + (int64_t)(m.start[sg.key_base + key] - base0) + slot, r);
+        }
+    }
+}
+
+__global__ void k_rec32_to_soa_multi(MultiSort m)
+{
+    __shared__ int32_t s_end[kMaxSortSegs];
+    const int nseg = *m.nseg;
+    const int32_t total = load_chunk_ends(m, s_end, nseg);
+    for (int64_t c = blockIdx.x; c < total; c += gridDim.x) {
+        const int si = find_seg(s_end, nseg, c);
+        const SortSeg &sg = m.segs[si];
+        const int64_t first = (c - (si > 0 ? s_end[si - 1] : 0)) * (int64_t)kSortChunk;
+        const int64_t last = min(first + (int64_t)kSortChunk, sg.count);
+        for (int64_t i = first + threadIdx.x; i < last; i += blockDim.x) {
+            const int64_t j = sg.off + i;
+            const int4 a = sg.rec[2 * j], b = sg.rec[2 * j + 1];
+            sg.p.cell[j] = a.x;
+            sg.p.ox[j] = __int_as_float(a.y); sg.p.oy[j] = __int_as_float(a.z); sg.p.oz[j] = __int_as_float(a.w);
+            sg.p.vx[j] = __int_as_float(b.x); sg.p.vy[j] = __int_as_float(b.y); sg.p.vz[j] = __int_as_float(b.z);
+            if (sg.ids) sg.ids[j] = (uint32_t)b.w;
         }
     }
 }
@@ -423,7 +442,8 @@ int launch_sort_finish_multi(cudaStream_t st, const MultiSort &m, int64_t chunks
     if (chunks > 0) {
         const int64_t grid = chunks < 152 * 8 ? chunks : 152 * 8;
         k_scatter_multi<<<(unsigned)grid, 256, 0, st>>>(m);
-        ++launches;
+        k_rec32_to_soa_multi<<<(unsigned)grid, 256, 0, st>>>(m);
+        launches += 2;
     }
     return launches;
 }
