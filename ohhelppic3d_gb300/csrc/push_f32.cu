@@ -681,10 +681,11 @@ __global__ void __launch_bounds__(256, 2) tiled_f32_multi(MultiPush m)
             cur = r;
             __syncthreads();
         }
-        // A private copy of the descriptor: its hot fields live in registers
-        // instead of being re-read from shared memory after every shared atomic.
-        const TileArgs a = sd.a;
-        const PartF32 p = sd.p;
+        // The descriptor is read in place from shared memory.  A private copy
+        // (about 1 KB per thread, its per-species arrays indexed at run time)
+        // lands in local memory and costs 256 KB of local stores per item.
+        const TileArgs &a = sd.a;
+        const PartF32 &p = sd.p;
         run_item<MODE, DEP, PPL>(a, p, nullptr, item - (r > 0 ? s_end[r - 1] : 0), smem, &ebar);
         __syncthreads();   // the next item reuses the shared boxes and descriptor
     }
