@@ -323,7 +323,10 @@ def sequential_runs(P, reqs, sort_every: int) -> dict:
         cfg = P.make_config(n=r.n, dt=r.dt, b0=r.b0, qm=r.qm, q=r.q, capacity=caps, precision=P.FP32,
                             sort_every=sort_every)
         with P.PicContext(cfg) as ctx:
-            ctx.set_tuning(halo=1)   # the server's launch shape
+            # the server's launch shape: halo 1, tile edges up to 16 in x and 8 in y, z
+            tile = tuple(max(t for t in (1, 2, 4, 8, 16) if t <= want and n % t == 0)
+                         for n, want in zip(r.n, (16, 8, 8)))
+            ctx.set_tuning(halo=1, tile=tile)
             counts = ctx.init_particles(r.species, seed=r.seed)
             ctx.synchronize()
             t1 = time.perf_counter()
@@ -467,7 +470,7 @@ def main(argv=None) -> int:
     ap.add_argument("--serve-only", action="store_true", help="only the ensemble serving measurement")
     ap.add_argument("--serve-runs", type=int, default=512)
     ap.add_argument("--serve-step-scale", type=float, default=0.1)
-    ap.add_argument("--serve-sort-every", type=int, default=20)
+    ap.add_argument("--serve-sort-every", type=int, default=8)
     ap.add_argument("--serve-sequential", type=int, default=32, help="runs timed one at a time")
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "ours":

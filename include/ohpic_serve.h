@@ -41,16 +41,19 @@ typedef struct {
     int32_t max_active;          /* runs on the GPU at once (<= 512; 0 = 512) */
     int64_t hbm_budget;          /* bytes for run state and field pools (0 = 60% of free memory) */
     int32_t slots_per_pool;      /* field slots per grid-size pool (0 = 16) */
-    int32_t sort_every;          /* ticks between cell sorts of all runs (0 = 20) */
+    int32_t sort_every;          /* ticks between cell sorts of all runs (0 = 8) */
     int32_t use_graphs;          /* 1: replay each tick as a captured CUDA graph */
     int32_t weights;             /* OHPIC_WEIGHTS_* for every run */
-    int32_t tile;                /* largest tile edge in cells (0 = 8); per grid, the largest power of two
-                                    <= tile dividing the edge */
+    int32_t tile;                /* largest tile edge in y and z (0 = 8); per grid, the largest power of
+                                    two <= tile dividing the edge */
     int32_t halo;                /* staged halo cells (0 = 1) */
     int32_t deposit;             /* OHPIC_DEPOSIT_* */
     int32_t max_species;         /* species per run the pools hold (0 = 2, <= OHPIC_MAX_SPECIES) */
     int32_t lane_particles;      /* consecutive particles per lane in the push, 2 or 4 (0 = 4) */
-    int32_t reserved[5];
+    int32_t tile_x;              /* largest tile edge along x (0 = 2 x tile, at most 64): a tile twice as
+                                    long in x halves the halo share of the staged box and still
+                                    leaves two CTAs per SM */
+    int32_t reserved[4];
 } ohpic_serve_config;
 
 typedef struct {
@@ -109,7 +112,7 @@ int ohpic_serve_result(ohpic_server *s, int64_t id, ohpic_run_result *res, doubl
 int ohpic_serve_release(ohpic_server *s, int64_t id);
 int ohpic_serve_stats_get(ohpic_server *s, ohpic_serve_stats *st);
 int ohpic_serve_last_error(ohpic_server *s, char *buf, size_t len);
-/* HBM bytes a run would hold while active (particles twice, sort and tile tables). */
+/* HBM bytes a run would hold while active (particles, a 32-byte sort record per slot, tile table). */
 int64_t ohpic_serve_footprint(const ohpic_serve_config *cfg, const ohpic_run_request *req);
 
 #ifdef __cplusplus

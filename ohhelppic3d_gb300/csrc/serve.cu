@@ -10,9 +10,9 @@
 //   particles  one persistent launch of tiled_f32_multi (push_f32.cu) over all
 //              runs: CTAs pull (run, species, tile) items from one queue ordered
 //              by decreasing particles per item.
-//   sort       every sort_every ticks, one histogram, one scan and one scatter
-//              over every (run, species) segment (sort.cu); the counters of all
-//              segments live in one key space laid out by pool slot.
+//   sort       every sort_every ticks, one histogram, one scan, one record scatter
+//              and one transpose over every (run, species) segment (sort.cu); the
+//              counters of all segments live in one key space laid out by pool slot.
 //
 // A tick's launches are captured into a CUDA graph (and a second graph for the
 // sort) and replayed until the set of grid-size pools in use changes: the tables
@@ -291,13 +291,22 @@ namespace {
 using Server = ohpic_server;
 
 // Geometry of a run's grid with the server's tile and halo (FP32 form).
+// Largest tile edges: y and z, then x.
+void tile_edges(const ohpic_serve_config &cfg, int &t, int &tx)
+{
+    t = cfg.tile > 0 ? cfg.tile : 8;
+    tx = cfg.tile_x > 0 ? cfg.tile_x : std::min(64, 2 * t);
+}
+
 bool serve_geom(const ohpic_serve_config &cfg, int nx, int ny, int nz, Geom &g)
 {
     ohpic_config k;
     ohpic_config_default(&k);
     k.nx = nx; k.ny = ny; k.nz = nz;
     k.precision = OHPIC_FP32;
-    const int tile[3] = {pick_tile(nx, cfg.tile), pick_tile(ny, cfg.tile), pick_tile(nz, cfg.tile)};
+    int t, tx;
+    tile_edges(cfg, t, tx);
+    const int tile[3] = {pick_tile(nx, tx), pick_tile(ny, t), pick_tile(nz, t)};
     if (tile[0] < 1 || tile[1] < 1 || tile[2] < 1) return false;
     return make_geom(k, tile, cfg.halo, g);
 }
@@ -552,7 +561,9 @@ bool upload_tables(Server *s, std::vector<Run *> &runs)
 void fixed_shapes(Server *s)
 {
     Geom g;
-    const int n = std::max(1, 2 * std::max(1, s->cfg.tile > 0 ? s->cfg.tile : 8));
+    int t, tx;
+    tile_edges(s->cfg, t, tx);
+    const int n = 2 * std::max(t, tx);   // the largest staged box any grid gets
     serve_geom(s->cfg, n, n, n, g);
     s->push_smem = (size_t)((((int64_t)g.sx * g.sy * g.sz * (16 + 8) + 15) & ~(int64_t)15) + 128 +
                             (s->cfg.lane_particles == 4 ? kQuadStageBytes : 0));
@@ -1070,7 +1081,7 @@ void ohpic_serve_config_default(ohpic_serve_config *cfg)
     memset(cfg, 0, sizeof(*cfg));
     cfg->max_active = kMaxServeRuns;
     cfg->slots_per_pool = 16;
-    cfg->sort_every = 20;
+    cfg->sort_every = 8;
     cfg->use_graphs = 1;
     cfg->weights = OHPIC_WEIGHTS_REFERENCE;
     cfg->halo = 1;
@@ -1104,10 +1115,10 @@ static bool normalise(const ohpic_serve_config *in, ohpic_serve_config &c)
     if (c.slots_per_pool <= 0) c.slots_per_pool = 16;
     if (c.slots_per_pool > 256) return false;
     if (c.sort_every < 0) return false;
-    if (c.sort_every == 0) c.sort_every = 20;
+    if (c.sort_every == 0) c.sort_every = 8;
     if (c.halo <= 0) c.halo = 1;
     if (c.halo > kMaxHalo) return false;
-    if (c.tile < 0 || c.tile > 64) return false;
+    if (c.tile < 0 || c.tile > 64 || c.tile_x < 0 || c.tile_x > 64) return false;
     if (c.max_species <= 0) c.max_species = 2;
     if (c.max_species > OHPIC_MAX_SPECIES) return false;
     if (c.lane_particles == 0) c.lane_particles = 4;

@@ -34,6 +34,22 @@ def test_serve_symbols_exported_and_bound(ohpic):
     assert sorted(S.SERVE_SIGNATURES) == names
 
 
+def test_config_struct_matches_header():
+    """The ctypes mirror of ohpic_serve_config has the header's fields, in order,
+    with the same integer widths and array lengths."""
+    from ohhelppic3d_gb300 import serve as S
+    with open(os.path.join(ROOT, "include", "ohpic_serve.h")) as f:
+        text = re.sub(r"/\*.*?\*/", "", f.read(), flags=re.S)
+    body = re.search(r"typedef struct \{([^}]*)\}\s*ohpic_serve_config;", text).group(1)
+    fields = re.findall(r"int(32|64)_t\s+(\w+)(?:\[(\d+)\])?;", body)
+    ctypes_of = {"32": C.c_int32, "64": C.c_int64}
+    mirror = S.ServeConfig._fields_
+    assert [f[1] for f in fields] == [m[0] for m in mirror]
+    for (bits, name, count), (mname, mtype) in zip(fields, mirror):
+        want = ctypes_of[bits] * int(count) if count else ctypes_of[bits]
+        assert C.sizeof(mtype) == C.sizeof(want), name
+
+
 def test_footprint_is_host_side(ohpic):
     from ohhelppic3d_gb300 import serve as S
     cfg = S.config()
