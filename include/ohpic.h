@@ -221,7 +221,10 @@ enum {
     OHPIC_DEPOSIT_RUNS = 0,       /* warp segmented reduction over runs of equal cells (shuffles) */
     OHPIC_DEPOSIT_UNIFORM = 1,    /* whole-warp hardware reduce when all lanes share a cell, else runs */
     OHPIC_DEPOSIT_MATCH = 2,      /* match lanes by cell, hardware reduce per group */
-    OHPIC_DEPOSIT_GROUPS = 3      /* one whole-warp hardware reduce per distinct cell (up to 3), then runs */
+    OHPIC_DEPOSIT_GROUPS = 3,     /* one whole-warp hardware reduce per distinct cell (up to 3), then runs */
+    OHPIC_DEPOSIT_LANES = 4       /* no warp combining: each lane adds its register sums to the shared box
+                                     (the default; with four particles per lane the same-address shared
+                                     atomics cost less than the shuffles) */
 };
 typedef struct ohpic_tuning {
     int32_t tile[3];            /* cells per tile edge; powers of two dividing n, <= 64 */

@@ -81,7 +81,7 @@ class Tuning(C.Structure):
                 "deposit": self.deposit, "sort_every": self.sort_every, "lane_particles": self.lane_particles}
 
 
-DEPOSIT_RUNS, DEPOSIT_UNIFORM, DEPOSIT_MATCH, DEPOSIT_GROUPS = 0, 1, 2, 3
+DEPOSIT_RUNS, DEPOSIT_UNIFORM, DEPOSIT_MATCH, DEPOSIT_GROUPS, DEPOSIT_LANES = 0, 1, 2, 3, 4
 
 
 class OhpicError(RuntimeError):

@@ -22,7 +22,8 @@ import json
 import os
 import time
 
-from . import DEPOSIT_GROUPS, DEPOSIT_MATCH, DEPOSIT_RUNS, DEPOSIT_UNIFORM, FP32, OhpicError, PicContext, make_config
+from . import (DEPOSIT_GROUPS, DEPOSIT_LANES, DEPOSIT_MATCH, DEPOSIT_RUNS, DEPOSIT_UNIFORM, FP32, OhpicError,
+               PicContext, make_config)
 
 
 def _divisors(n: int) -> list:
@@ -122,7 +123,7 @@ def tune(n, dt, b0, qm, q, capacity_per_cell, species, precision=FP32, weights=0
     try:
         if precision == FP32:
             descend("lane_particles", [2, 4])
-            descend("deposit", [DEPOSIT_RUNS, DEPOSIT_GROUPS, DEPOSIT_UNIFORM, DEPOSIT_MATCH])
+            descend("deposit", [DEPOSIT_LANES, DEPOSIT_RUNS, DEPOSIT_GROUPS, DEPOSIT_UNIFORM, DEPOSIT_MATCH])
         # tile and halo together: the halo's absolute width sets how far particles
         # drift before they leave the staged box, and with the tile it sets the
         # shared memory per CTA, so a small tile with a wide halo can beat both a

@@ -304,7 +304,7 @@ int ohpic_create(const ohpic_config *cfg, ohpic_ctx **out)
     c->split = 1;
     c->with_energy = false;
     c->sc_dt = NAN;
-    c->dep_strategy = OHPIC_DEPOSIT_RUNS;
+    c->dep_strategy = OHPIC_DEPOSIT_LANES;
     c->lane_particles = 4;
     Geom &g = c->g;
     if (!make_geom(k, tile, c->halo, g)) {
@@ -795,7 +795,7 @@ int ohpic_get_tuning(ohpic_ctx *c, ohpic_tuning *t)
 int ohpic_set_tuning(ohpic_ctx *c, const ohpic_tuning *t)
 {
     if (!c || !t) return OHPIC_ERR_INVALID;
-    if (t->split < 1 || t->split > 64 || t->deposit < OHPIC_DEPOSIT_RUNS || t->deposit > OHPIC_DEPOSIT_GROUPS ||
+    if (t->split < 1 || t->split > 64 || t->deposit < OHPIC_DEPOSIT_RUNS || t->deposit > OHPIC_DEPOSIT_LANES ||
         t->sort_every < 0 || (t->lane_particles != 2 && t->lane_particles != 4))
         return fail(c, OHPIC_ERR_INVALID,
                     "tuning: split 1..64, deposit 0..3, sort_every >= 0, lane_particles 2 or 4");

@@ -9,22 +9,24 @@
 // Particle state: int32 packed cell (ix | iy<<11 | iz<<22), FP32 offsets in
 // [0, 1) and FP32 velocities, 28 bytes per particle in 7 SoA arrays.
 //
-// Mapping.  Lane l of a warp handles particles base + 2l and base + 2l + 1, so
-// the 32 lanes hold 64 consecutive particles of the cell-sorted order: their cells are mostly the
-// same one or two, the 8 node loads of the gather are shared-memory broadcasts,
-// and their deposits form runs of equal cells across adjacent lanes.  Loads and
-// stores are 8-byte vector accesses coalesced across the warp; the next pair's
-// 7 vectors are loaded before the current pair is computed.
+// Mapping.  Lane l of a warp handles four consecutive particles (base + 4l ..
+// base + 4l + 3; two as a tunable), so the 32 lanes hold 128 consecutive
+// particles of the cell-sorted order: their cells are mostly the same few, and
+// the 8 node loads of the gather are shared-memory broadcasts.  Loads and stores
+// are 16-byte vector accesses coalesced across the warp; the next quad is
+// prefetched into shared memory while the current one is computed.
 //
 // Deposit in fixed point.  Each particle's 8 CIC weights are integers in units of
 // 2^-24 that sum to exactly 2^24 (an exact axis-by-axis split; charge is
-// conserved exactly).  A warp segmented reduction (integer shuffles, at most 5
-// steps, stopping early when runs are short) sums each run into its first lane,
-// which adds the sums to a shared 64-bit box kept as 32-bit low/high words:
-// 32-bit shared atomic adds are native and same-address adds within a warp do not
-// serialise, unlike FP32 shared atomics.  The box is flushed once per CTA into
-// per-species 64-bit global sums.  All of it is integer addition, so the deposit
-// does not depend on the order in which atomics land.
+// conserved exactly).  A lane sums the weights of its consecutive same-cell
+// particles in registers and adds them to a shared 64-bit box kept as 32-bit
+// low/high words: 32-bit shared atomic adds are native, unlike FP32 shared
+// atomics.  By default (OHPIC_DEPOSIT_LANES) the lanes add directly; warp
+// combinations before the add (segmented shuffles over runs of equal cells,
+// hardware reduces) are tunable alternatives that measured slower with four
+// particles per lane.  The box is flushed once per CTA into per-species 64-bit
+// global sums.  All of it is integer addition, so the deposit does not depend on
+// the order in which atomics land.
 #include <type_traits>
 
 #include "tile_common.cuh"
@@ -71,15 +73,19 @@ __device__ __forceinline__ void box_add8(unsigned *hi, unsigned *lo, int key, in
         if (old[v] + u[v] < old[v]) atomicAdd(hi + key + off[v], 1u);
 }
 
-// Adds u (weights, key = box index of the cell or < 0) to the shared box after
-// combining the lanes that share a key.  DEP picks the combination
-// (OHPIC_DEPOSIT_*): runs of adjacent lanes by shuffles; one hardware warp
-// reduce when every lane holds the same key, else runs; or __match_any_sync
-// groups reduced with __reduce_add_sync.  All 32 lanes must call this.
+// Adds u (weights, key = box index of the cell or < 0) to the shared box.  DEP
+// picks how lanes that share a key are combined first (OHPIC_DEPOSIT_*): not at
+// all (LANES); runs of adjacent lanes by shuffles; one hardware warp reduce when
+// every lane holds the same key, else runs; or __match_any_sync groups reduced
+// with __reduce_add_sync.  All 32 lanes must call this.
 template <int DEP>
 __device__ __forceinline__ void warp_run_deposit(int key, unsigned u[8], unsigned *lo, unsigned *hi, int sx,
                                                  int sxy)
 {
+    if (DEP == OHPIC_DEPOSIT_LANES) {
+        if (key >= 0) box_add8(hi, lo, key, sx, sxy, u);
+        return;
+    }
     const unsigned lane = threadIdx.x & 31u;
     bool head;
     if (DEP == OHPIC_DEPOSIT_GROUPS) {
@@ -712,6 +718,7 @@ static auto by_deposit(int dep, F f)
     case OHPIC_DEPOSIT_MATCH: return f(std::integral_constant<int, OHPIC_DEPOSIT_MATCH>());
     case OHPIC_DEPOSIT_UNIFORM: return f(std::integral_constant<int, OHPIC_DEPOSIT_UNIFORM>());
     case OHPIC_DEPOSIT_GROUPS: return f(std::integral_constant<int, OHPIC_DEPOSIT_GROUPS>());
+    case OHPIC_DEPOSIT_LANES: return f(std::integral_constant<int, OHPIC_DEPOSIT_LANES>());
     default: return f(std::integral_constant<int, OHPIC_DEPOSIT_RUNS>());
     }
 }

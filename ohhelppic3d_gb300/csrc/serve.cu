@@ -1085,7 +1085,7 @@ void ohpic_serve_config_default(ohpic_serve_config *cfg)
     cfg->use_graphs = 1;
     cfg->weights = OHPIC_WEIGHTS_REFERENCE;
     cfg->halo = 1;
-    cfg->deposit = OHPIC_DEPOSIT_RUNS;
+    cfg->deposit = OHPIC_DEPOSIT_LANES;
     cfg->max_species = 2;
 }
 
@@ -1124,7 +1124,7 @@ static bool normalise(const ohpic_serve_config *in, ohpic_serve_config &c)
     if (c.lane_particles == 0) c.lane_particles = 4;
     if (c.lane_particles != 2 && c.lane_particles != 4) return false;
     if (c.weights != OHPIC_WEIGHTS_REFERENCE && c.weights != OHPIC_WEIGHTS_STANDARD) return false;
-    if (c.deposit < OHPIC_DEPOSIT_RUNS || c.deposit > OHPIC_DEPOSIT_GROUPS) return false;
+    if (c.deposit < OHPIC_DEPOSIT_RUNS || c.deposit > OHPIC_DEPOSIT_LANES) return false;
     return true;
 }
 

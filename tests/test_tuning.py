@@ -46,6 +46,7 @@ def test_fp32_state_identical_across_launch_shapes(ohpic):
     P = ohpic
     ref_f, ref_p, ref_d = _run(P, {})
     variants = [{"deposit": P.DEPOSIT_UNIFORM}, {"deposit": P.DEPOSIT_MATCH}, {"deposit": P.DEPOSIT_GROUPS},
+                {"deposit": P.DEPOSIT_RUNS}, {"lane_particles": 2, "deposit": P.DEPOSIT_LANES},
                 {"tile": (4, 4, 4)}, {"tile": (16, 8, 8), "deposit": P.DEPOSIT_GROUPS}, {"halo": 1},
                 {"halo": 3}, {"split": 3}, {"sort_every": 1}, {"sort_every": 100},
                 {"lane_particles": 2}, {"lane_particles": 2, "deposit": P.DEPOSIT_UNIFORM},
@@ -94,4 +95,4 @@ def test_autotuner_returns_a_valid_shape(ohpic):
                capacity_per_cell=[2 * ppc, 2 * ppc], species=sp, precision=P.FP32, steps=2, max_cadence=8)
     assert all(32 % t["tile"][d] == 0 for d in range(3))
     assert 0 <= t["halo"] <= 4 and t["split"] >= 1 and t["sort_every"] >= 1
-    assert t["deposit"] in (P.DEPOSIT_RUNS, P.DEPOSIT_UNIFORM, P.DEPOSIT_MATCH, P.DEPOSIT_GROUPS)
+    assert t["deposit"] in (P.DEPOSIT_RUNS, P.DEPOSIT_UNIFORM, P.DEPOSIT_MATCH, P.DEPOSIT_GROUPS, P.DEPOSIT_LANES)
