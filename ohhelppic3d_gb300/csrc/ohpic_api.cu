@@ -59,11 +59,16 @@ bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g)
     g.tile_cells = g.tx * g.ty * g.tz;
     g.nxh = g.nx / 2 + 1;
     g.nspec = (int64_t)g.nxh * g.ny * g.nz;
+    // The FP32 deposit box reaches one cell further than the staged E box: at
+    // 8 bytes per node it is cheap, and it keeps the deposits of particles that
+    // drifted just outside the E box in shared memory.
+    g.dhalo = k.precision == OHPIC_FP64 ? halo : halo + 1;
+    g.dsx = g.tx + 2 * g.dhalo + 1; g.dsy = g.ty + 2 * g.dhalo + 1; g.dsz = g.tz + 2 * g.dhalo + 1;
     // Staged E box (4 reals per node) plus the deposit box (8 bytes per node).
-    const int64_t s3 = (int64_t)g.sx * g.sy * g.sz;
+    const int64_t s3 = (int64_t)g.sx * g.sy * g.sz, s3d = (int64_t)g.dsx * g.dsy * g.dsz;
     const int64_t es = k.precision == OHPIC_FP64 ? 8 : 4;
     // (leaves room for the FP32 push's 28 KB prefetch stage within a CTA's 227 KB)
-    return s3 * (4 * es + 8) <= 192 * 1024;
+    return s3 * 4 * es + s3d * 8 <= 192 * 1024;
 }
 
 // Boris constants of one species for a time step (particle_mover_boris.f90:37-43),

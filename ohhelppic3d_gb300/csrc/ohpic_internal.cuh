@@ -55,6 +55,8 @@ struct Geom {
     int ntx, nty, ntz;     // tiles per axis
     int halo;              // cells staged around a tile
     int sx, sy, sz;        // staged nodes per axis: t + 2*halo + 1
+    int dhalo;             // cells of the deposit box around a tile (FP32 form: halo + 1)
+    int dsx, dsy, dsz;     // deposit box nodes per axis: t + 2*dhalo + 1
     int gx, gy, gz;        // padded E nodes per axis: n + 2*halo + 1
     int64_t ncell;
     int64_t ntile;

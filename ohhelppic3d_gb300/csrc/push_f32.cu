@@ -176,19 +176,22 @@ __device__ __forceinline__ void stage_f32(const TileArgs &a, const Item &it, flo
 {
     // One box row (fixed y, z) per warp iteration, lanes along x.
     const Geom &g = a.g;
-    const float4 *E = (const float4 *)a.epad;
-    const int rows = g.sy * g.sz, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int r = threadIdx.x >> 5; r < rows; r += nw) {
-        const int cz = r / g.sy, by = r - cz * g.sy;
-        // padded index of node x0 - halo + ax is x0 + ax
-        const float4 *src = E + ((int64_t)(it.z0 + cz) * g.gy + (it.y0 + by)) * g.gx + it.x0;
-        const int base = r * g.sx;
-        for (int ax = lane; ax < g.sx; ax += 32) {
-            if (need_e) sE[base + ax] = __ldg(src + ax);
-            if (need_w) {
-                lo[base + ax] = 0u;
-                hi[base + ax] = 0u;
-            }
+    if (need_e) {
+        const float4 *E = (const float4 *)a.epad;
+        const int rows = g.sy * g.sz, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+        for (int r = threadIdx.x >> 5; r < rows; r += nw) {
+            const int cz = r / g.sy, by = r - cz * g.sy;
+            // padded index of node x0 - halo + ax is x0 + ax
+            const float4 *src = E + ((int64_t)(it.z0 + cz) * g.gy + (it.y0 + by)) * g.gx + it.x0;
+            const int base = r * g.sx;
+            for (int ax = lane; ax < g.sx; ax += 32) sE[base + ax] = __ldg(src + ax);
+        }
+    }
+    if (need_w) {
+        const int s3d = g.dsx * g.dsy * g.dsz;
+        for (int i = threadIdx.x; i < s3d; i += blockDim.x) {
+            lo[i] = 0u;
+            hi[i] = 0u;
         }
     }
 }
@@ -197,17 +200,17 @@ __device__ __forceinline__ void flush_f32(const TileArgs &a, const Item &it, con
 {
     const Geom &g = a.g;
     unsigned long long *w = a.wsum + (int64_t)it.sp * g.ncell;
-    const int rows = g.sy * g.sz, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int rows = g.dsy * g.dsz, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int r = threadIdx.x >> 5; r < rows; r += nw) {
-        const int cz = r / g.sy, by = r - cz * g.sy;
-        const int y = wrapi(it.y0 - g.halo + by, g.ny);
-        const int z = wrapi(it.z0 - g.halo + cz, g.nz);
+        const int cz = r / g.dsy, by = r - cz * g.dsy;
+        const int y = wrapi(it.y0 - g.dhalo + by, g.ny);
+        const int z = wrapi(it.z0 - g.dhalo + cz, g.nz);
         unsigned long long *row = w + (int64_t)g.nx * (y + (int64_t)g.ny * z);
-        const int base = r * g.sx;
-        for (int ax = lane; ax < g.sx; ax += 32) {
+        const int base = r * g.dsx;
+        for (int ax = lane; ax < g.dsx; ax += 32) {
             const unsigned long long v = ((unsigned long long)hi[base + ax] << 32) | lo[base + ax];
             if (v) {
-                int x = it.x0 - g.halo + ax;
+                int x = it.x0 - g.dhalo + ax;
                 if ((unsigned)x >= (unsigned)g.nx) x = wrapi(x, g.nx);
                 atomicAdd(row + x, v);
             }
@@ -359,7 +362,8 @@ struct Tally {
 // or -1 when there is no shared deposit (no deposit mode, outside the box: then
 // the weights already went to global memory, or an invalid cell).
 template <int MODE>
-__device__ __forceinline__ int advance(const TileArgs &a, const Box &box, bool e_ok, const float4 *sE, int sp,
+__device__ __forceinline__ int advance(const TileArgs &a, const Box &box, const Box &dbox, bool e_ok,
+                                       const float4 *sE, int sp,
                                        const Push32 &k, int64_t idx, P32 &s, unsigned u[8], Tally &t)
 {
     constexpr bool kGather = MODE != MODE_DEPOSIT;
@@ -427,7 +431,7 @@ __device__ __forceinline__ int advance(const TileArgs &a, const Box &box, bool e
     }
     if (!kDeposit) return -1;
     fixed_weights(a.weights, s.ox, s.oy, s.oz, u);
-    const int dkey = box.key(ix, iy, iz);
+    const int dkey = dbox.key(ix, iy, iz);
     if (dkey < 0) {
         deposit_global_fixed(g, a.wsum + (int64_t)sp * g.ncell, ix, iy, iz, u);
         if (!kGather) ++t.out;
@@ -453,11 +457,11 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
     constexpr bool kDeposit = MODE == MODE_PUSH || MODE == MODE_DEPOSIT;
 
     const Geom &g = a.g;
-    const Box box = make_box(g, it);
-    const int s3 = g.sx * g.sy * g.sz;
+    const Box box = make_box(g, it), dbox = make_dbox(g, it);
+    const int s3 = g.sx * g.sy * g.sz, s3d = g.dsx * g.dsy * g.dsz;
     float4 *sE = (float4 *)smem;
     unsigned *slo = (unsigned *)(smem + (kGather ? (size_t)s3 * sizeof(float4) : 0));
-    unsigned *shi = slo + s3;
+    unsigned *shi = slo + s3d;
     // The E box arrives by one TMA copy while the threads clear the deposit box.
     const bool tma = box.on && kGather && a.use_tma && emap != nullptr;
     if (tma && threadIdx.x == 0) {
@@ -500,8 +504,8 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
 #pragma unroll
         for (int v = 0; v < 8; ++v) u0[v] = u1[v] = 0u;
         if (gv) {
-            if (2 * gi < end) k0 = advance<MODE>(a, box, e_ok, sE, sp, k, 2 * gi, cur[0], u0, t);
-            if (2 * gi + 1 < end) k1 = advance<MODE>(a, box, e_ok, sE, sp, k, 2 * gi + 1, cur[1], u1, t);
+            if (2 * gi < end) k0 = advance<MODE>(a, box, dbox, e_ok, sE, sp, k, 2 * gi, cur[0], u0, t);
+            if (2 * gi + 1 < end) k1 = advance<MODE>(a, box, dbox, e_ok, sE, sp, k, 2 * gi + 1, cur[1], u1, t);
             if (kMove) store_pair(p, gi, cur);
         }
         if (kDeposit) {
@@ -510,8 +514,8 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
                 for (int v = 0; v < 8; ++v) u0[v] += u1[v];
                 k1 = -1;
             }
-            warp_run_deposit<DEP>(k0, u0, slo, shi, box.sx, box.sxy);
-            if (__any_sync(kFull, k1 >= 0)) warp_run_deposit<DEP>(k1, u1, slo, shi, box.sx, box.sxy);
+            warp_run_deposit<DEP>(k0, u0, slo, shi, dbox.sx, dbox.sxy);
+            if (__any_sync(kFull, k1 >= 0)) warp_run_deposit<DEP>(k1, u1, slo, shi, dbox.sx, dbox.sxy);
         }
         gi = gn;
         gv = vn;
@@ -541,11 +545,11 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
     constexpr bool kMove = MODE == MODE_PUSH;
 
     const Geom &g = a.g;
-    const Box box = make_box(g, it);
-    const int s3 = g.sx * g.sy * g.sz;
+    const Box box = make_box(g, it), dbox = make_dbox(g, it);
+    const int s3 = g.sx * g.sy * g.sz, s3d = g.dsx * g.dsy * g.dsz;
     float4 *sE = (float4 *)smem;
     unsigned *slo = (unsigned *)(smem + (kGather ? (size_t)s3 * sizeof(float4) : 0));
-    unsigned *shi = slo + s3;
+    unsigned *shi = slo + s3d;
     const bool tma = box.on && kGather && a.use_tma && emap != nullptr;
     if (tma && threadIdx.x == 0) {
         mbar_init(ebar, 1);
@@ -572,7 +576,7 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
     const int64_t end = a.seg[sp] + a.count[sp];
     Tally t;
     // Prefetch stage after the boxes (16-byte aligned); the launch reserves it.
-    const size_t boxes = box.on ? ((kGather ? (size_t)s3 * sizeof(float4) : 0) + (size_t)s3 * 8 + 15) & ~(size_t)15 : 0;
+    const size_t boxes = box.on ? ((kGather ? (size_t)s3 * sizeof(float4) : 0) + (size_t)s3d * 8 + 15) & ~(size_t)15 : 0;
     float4 *stage = (float4 *)(smem + boxes);
     if (it.g0 + threadIdx.x < it.g1) prefetch_quad<kGather>(stage, p, it.g0 + threadIdx.x);
 
@@ -590,10 +594,10 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
             for (int j = 0; j < 4; ++j) {
                 if (4 * gi + j < end) {
                     unsigned u[8];
-                    const int kk = advance<MODE>(a, box, e_ok, sE, sp, k, 4 * gi + j, q[j], u, t);
+                    const int kk = advance<MODE>(a, box, dbox, e_ok, sE, sp, k, 4 * gi + j, q[j], u, t);
                     if (kk >= 0) {
                         if (kk != acc_key) {
-                            if (acc_key >= 0) box_add8(shi, slo, acc_key, box.sx, box.sxy, acc);
+                            if (acc_key >= 0) box_add8(shi, slo, acc_key, dbox.sx, dbox.sxy, acc);
                             acc_key = kk;
 #pragma unroll
                             for (int v = 0; v < 8; ++v) acc[v] = u[v];
@@ -606,7 +610,7 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
             }
             if (kMove) store_quad(p, gi, q);
         }
-        warp_run_deposit<DEP>(acc_key, acc, slo, shi, box.sx, box.sxy);
+        warp_run_deposit<DEP>(acc_key, acc, slo, shi, dbox.sx, dbox.sxy);
     }
     if (box.on) {
         __syncthreads();

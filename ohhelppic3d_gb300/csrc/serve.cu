@@ -565,7 +565,8 @@ void fixed_shapes(Server *s)
     tile_edges(s->cfg, t, tx);
     const int n = 2 * std::max(t, tx);   // the largest staged box any grid gets
     serve_geom(s->cfg, n, n, n, g);
-    s->push_smem = (size_t)((((int64_t)g.sx * g.sy * g.sz * (16 + 8) + 15) & ~(int64_t)15) + 128 +
+    s->push_smem = (size_t)((((int64_t)g.sx * g.sy * g.sz * 16 + (int64_t)g.dsx * g.dsy * g.dsz * 8 + 15) &
+                             ~(int64_t)15) + 128 +
                             (s->cfg.lane_particles == 4 ? kQuadStageBytes : 0));
     s->push_grid = s->sms * 2;
     int64_t nt = 0;
