@@ -193,6 +193,23 @@ int ohpic_upload_field(ohpic_ctx *ctx, int which, const double *host);
 int ohpic_download_field_ohfield(ohpic_ctx *ctx, int which, double *values, int nelem,
                                  const int32_t lo[3], const int32_t hi[3]);
 
+/* Checkpoint and restart of the particle state: the restart the reference's
+ * [continuaus] parameters describe (parameters.f90:91-94) but never implement.
+ * A snapshot is a byte image in host memory, written by the caller wherever it
+ * likes: a 256-byte header, then per species the particle arrays in the
+ * context's own form, bit for bit (FP32 form: packed cell, 3 offsets, 3
+ * velocities, id = 32 bytes per particle; FP64 form: 6 doubles and the id =
+ * 52 bytes, padded to 8).  The header holds the grid, form, species count, the
+ * per-species counts and the step counters; the physics (qm, q, B0, dt) comes
+ * from the restoring context's own config.  After a restore the next step
+ * deposits the restored particles again, so an FP32 run continues bit-identically
+ * (its deposit is integer); an FP64 run continues within FP64 atomic rounding.
+ * ohpic_snapshot_load() requires the same grid, form and species count, and
+ * counts within the context's capacities. */
+int ohpic_snapshot_size(ohpic_ctx *ctx, int64_t *bytes);
+int ohpic_snapshot_save(ohpic_ctx *ctx, void *host, int64_t bytes);
+int ohpic_snapshot_load(ohpic_ctx *ctx, const void *host, int64_t bytes);
+
 int ohpic_diagnostics(ohpic_ctx *ctx, ohpic_diag *out);
 /* With tracking on, the fused push also sums |v|^2 and v per species, so a
  * per-step ohpic_diagnostics reads them instead of making a second pass over

@@ -113,6 +113,9 @@ SIGNATURES = {
     "ohpic_push": (C.c_int, [_P, C.c_double]),
     "ohpic_step": (C.c_int, [_P, C.c_double, C.c_int]),
     "ohpic_sort": (C.c_int, [_P]),
+    "ohpic_snapshot_size": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "ohpic_snapshot_save": (C.c_int, [_P, C.c_void_p, C.c_int64]),
+    "ohpic_snapshot_load": (C.c_int, [_P, C.c_void_p, C.c_int64]),
     "ohpic_download_field": (C.c_int, [_P, C.c_int, _DP]),
     "ohpic_upload_field": (C.c_int, [_P, C.c_int, _DP]),
     "ohpic_download_field_ohfield": (C.c_int, [_P, C.c_int, _DP, C.c_int,
@@ -267,6 +270,20 @@ class PicContext:
                 perm = np.argsort(res["ids"], kind="stable")
                 res = {k: v[perm] for k, v in res.items()}
         return res
+
+    # -- checkpoint / restart ------------------------------------------------
+    def snapshot(self) -> bytes:
+        """The particle state and step counters as a byte image (ohpic_snapshot_save)."""
+        n = C.c_int64()
+        self._check(lib().ohpic_snapshot_size(self.ptr, C.byref(n)))
+        buf = np.empty(n.value, dtype=np.uint8)
+        self._check(lib().ohpic_snapshot_save(self.ptr, buf.ctypes.data_as(C.c_void_p), n.value))
+        return buf.tobytes()
+
+    def restore(self, snap: bytes):
+        """Replaces the particle state with a snapshot (ohpic_snapshot_load)."""
+        arr = np.frombuffer(snap, dtype=np.uint8)
+        self._check(lib().ohpic_snapshot_load(self.ptr, arr.ctypes.data_as(C.c_void_p), arr.size))
 
     def download_into(self, species: int, out: dict, ids: np.ndarray | None = None) -> int:
         """Device-order download into caller-provided float64 arrays (e.g. pinned host memory)."""

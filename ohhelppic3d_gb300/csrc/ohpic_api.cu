@@ -215,6 +215,49 @@ int do_push(ohpic_ctx *c, double dt)
     return OHPIC_OK;
 }
 
+// ---- checkpoint / restart: snapshot byte image ----
+const char kSnapMagic[8] = {'O', 'H', 'P', 'I', 'C', 'S', 'N', '1'};
+
+struct SnapHeader {
+    char magic[8];
+    int32_t version, precision, nx, ny, nz, nspecies, track_ids, reserved;
+    int64_t steps, steps_since_sort;
+    int64_t count[OHPIC_MAX_SPECIES];
+    char pad[256 - 8 - 8 * 4 - 2 * 8 - 8 * OHPIC_MAX_SPECIES];
+};
+static_assert(sizeof(SnapHeader) == 256, "snapshot header is 256 bytes");
+
+// Bytes of one species' arrays: FP32 7 words + id; FP64 6 doubles + id, padded to 8.
+int64_t snap_species_bytes(bool f64, int64_t n)
+{
+    return f64 ? (52 * n + 7) / 8 * 8 : 32 * n;
+}
+
+// The species' device arrays in snapshot order (byte addresses of element seg)
+// and their element sizes; returns the count.
+int snap_arrays(ohpic_ctx *c, int s, char *arr[7], int64_t es[7])
+{
+    const int64_t seg = c->seg[s];
+    if (c->cfg.precision == OHPIC_FP64) {
+        const PartF64 &q = c->p64[c->cur];
+        double *a[6] = {q.x, q.y, q.z, q.vx, q.vy, q.vz};
+        for (int k = 0; k < 6; ++k) {
+            arr[k] = (char *)(a[k] + seg);
+            es[k] = 8;
+        }
+        return 6;
+    }
+    const PartF32 &q = c->p32[c->cur];
+    arr[0] = (char *)(q.cell + seg);
+    es[0] = 4;
+    float *a[6] = {q.ox, q.oy, q.oz, q.vx, q.vy, q.vz};
+    for (int k = 0; k < 6; ++k) {
+        arr[k + 1] = (char *)(a[k] + seg);
+        es[k + 1] = 4;
+    }
+    return 7;
+}
+
 }  // namespace
 
 extern "C" {
@@ -838,6 +881,108 @@ int ohpic_set_tuning(ohpic_ctx *c, const ohpic_tuning *t)
     c->lane_particles = t->lane_particles;
     c->cfg.sort_every = t->sort_every;
     return OHPIC_OK;
+}
+
+int ohpic_snapshot_size(ohpic_ctx *c, int64_t *bytes)
+{
+    if (!c || !bytes) return fail(c, OHPIC_ERR_INVALID, "snapshot_size: null argument");
+    const bool f64 = c->cfg.precision == OHPIC_FP64;
+    int64_t b = (int64_t)sizeof(SnapHeader);
+    for (int s = 0; s < c->cfg.nspecies; ++s) b += snap_species_bytes(f64, c->count[s]);
+    *bytes = b;
+    return OHPIC_OK;
+}
+
+int ohpic_snapshot_save(ohpic_ctx *c, void *host, int64_t bytes)
+{
+    if (!c || !host) return fail(c, OHPIC_ERR_INVALID, "snapshot_save: null argument");
+    int64_t need = 0;
+    ohpic_snapshot_size(c, &need);
+    if (bytes < need) return fail(c, OHPIC_ERR_CAPACITY, "snapshot_save: buffer smaller than ohpic_snapshot_size");
+    cudaSetDevice(c->dev);
+    const bool f64 = c->cfg.precision == OHPIC_FP64;
+    SnapHeader h;
+    memset(&h, 0, sizeof(h));
+    memcpy(h.magic, kSnapMagic, sizeof(h.magic));
+    h.version = 1;
+    h.precision = c->cfg.precision;
+    h.nx = c->cfg.nx; h.ny = c->cfg.ny; h.nz = c->cfg.nz;
+    h.nspecies = c->cfg.nspecies;
+    h.track_ids = c->cfg.track_ids ? 1 : 0;
+    h.steps = c->steps;
+    h.steps_since_sort = c->steps_since_sort;
+    for (int s = 0; s < c->cfg.nspecies; ++s) h.count[s] = c->count[s];
+    memcpy(host, &h, sizeof(h));
+    char *p = (char *)host + sizeof(h);
+    for (int s = 0; s < c->cfg.nspecies; ++s) {
+        const int64_t n = c->count[s];
+        const int64_t sb = snap_species_bytes(f64, n);
+        char *arr[7];
+        int64_t es[7];
+        const int na = snap_arrays(c, s, arr, es);
+        memset(p, 0, (size_t)sb);   // ids when not tracked, and the FP64 padding
+        int64_t off = 0;
+        for (int k = 0; k < na && n > 0; ++k) {
+            OHPIC_CUDA_TRY(c, cudaMemcpyAsync(p + off, arr[k], (size_t)(es[k] * n), cudaMemcpyDeviceToHost, c->stream));
+            off += es[k] * n;
+        }
+        if (n > 0 && c->ids[c->cur])
+            OHPIC_CUDA_TRY(c, cudaMemcpyAsync(p + off, c->ids[c->cur] + c->seg[s], sizeof(uint32_t) * n,
+                                              cudaMemcpyDeviceToHost, c->stream));
+        p += sb;
+    }
+    OHPIC_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return check_device(c);
+}
+
+int ohpic_snapshot_load(ohpic_ctx *c, const void *host, int64_t bytes)
+{
+    if (!c || !host) return fail(c, OHPIC_ERR_INVALID, "snapshot_load: null argument");
+    if (bytes < (int64_t)sizeof(SnapHeader)) return fail(c, OHPIC_ERR_INVALID, "snapshot_load: truncated snapshot");
+    SnapHeader h;
+    memcpy(&h, host, sizeof(h));
+    if (memcmp(h.magic, kSnapMagic, sizeof(h.magic)) != 0 || h.version != 1)
+        return fail(c, OHPIC_ERR_INVALID, "snapshot_load: not an ohpic snapshot (magic or version)");
+    if (h.precision != c->cfg.precision || h.nx != c->cfg.nx || h.ny != c->cfg.ny || h.nz != c->cfg.nz ||
+        h.nspecies != c->cfg.nspecies)
+        return fail(c, OHPIC_ERR_INVALID, "snapshot_load: grid, precision form or species count differ");
+    if (c->cfg.track_ids && !h.track_ids)
+        return fail(c, OHPIC_ERR_INVALID, "snapshot_load: the context tracks ids but the snapshot has none");
+    const bool f64 = c->cfg.precision == OHPIC_FP64;
+    int64_t need = (int64_t)sizeof(SnapHeader);
+    for (int s = 0; s < h.nspecies; ++s) {
+        if (h.count[s] < 0 || h.count[s] > c->cap[s])
+            return fail(c, OHPIC_ERR_CAPACITY, "snapshot_load: species " + std::to_string(s) + " count " +
+                                                   std::to_string(h.count[s]) + " exceeds the capacity");
+        need += snap_species_bytes(f64, h.count[s]);
+    }
+    if (bytes < need) return fail(c, OHPIC_ERR_INVALID, "snapshot_load: truncated snapshot");
+    cudaSetDevice(c->dev);
+    const char *p = (const char *)host + sizeof(h);
+    for (int s = 0; s < h.nspecies; ++s) {
+        const int64_t n = h.count[s];
+        char *arr[7];
+        int64_t es[7];
+        const int na = snap_arrays(c, s, arr, es);
+        int64_t off = 0;
+        for (int k = 0; k < na && n > 0; ++k) {
+            OHPIC_CUDA_TRY(c, cudaMemcpyAsync(arr[k], p + off, (size_t)(es[k] * n), cudaMemcpyHostToDevice, c->stream));
+            off += es[k] * n;
+        }
+        if (n > 0 && c->ids[c->cur])
+            OHPIC_CUDA_TRY(c, cudaMemcpyAsync(c->ids[c->cur] + c->seg[s], p + off, sizeof(uint32_t) * n,
+                                              cudaMemcpyHostToDevice, c->stream));
+        c->count[s] = n;
+        p += snap_species_bytes(f64, n);
+    }
+    OHPIC_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    c->steps = h.steps;
+    c->steps_since_sort = h.steps_since_sort;
+    c->sorted = false;        // the next step sorts, then deposits the restored particles
+    c->rho_valid = false;
+    c->field_valid = false;
+    c->kin_valid = false;
+    return check_device(c);
 }
 
 }  // extern "C"
