@@ -296,10 +296,7 @@ int ohpic_destroy(ohpic_ctx *c)
     cudaSetDevice(c->dev);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (int b = 0; b < 2; ++b) {
-        dfree(c->p64[b].x); dfree(c->p64[b].y); dfree(c->p64[b].z);
-        dfree(c->p64[b].vx); dfree(c->p64[b].vy); dfree(c->p64[b].vz);
-        if (c->p32_block[b]) dfree(c->p32_block[b]);   // holds p32[b] and ids[b]
-        else dfree(c->ids[b]);
+        dfree(c->pblock[b]);   // holds the particle arrays and the ids
     }
     dfree(c->rho); dfree(c->phi); dfree(c->epad); dfree(c->spec); dfree(c->green); dfree(c->wsum);
     dfree(c->cell_count); dfree(c->cell_start); dfree(c->scan_tmp); dfree(c->tile_begin);
@@ -374,21 +371,21 @@ int ohpic_create(const ohpic_config *cfg, ohpic_ctx **out)
     int rc = OHPIC_OK;
     const int64_t N = c->total_slots;
     for (int b = 0; b < 2 && rc == OHPIC_OK; ++b) {
+        // eight arrays of N elements of the form's width in one block (N sort records)
+        const int64_t part = align_up(N * es, 256);
+        rc = dalloc(c, (char **)&c->pblock[b], 8 * part);
+        if (rc != OHPIC_OK) break;
+        char *base = (char *)c->pblock[b];
         if (f64) {
             double **arr[6] = {&c->p64[b].x, &c->p64[b].y, &c->p64[b].z, &c->p64[b].vx, &c->p64[b].vy, &c->p64[b].vz};
-            for (int a = 0; a < 6 && rc == OHPIC_OK; ++a) rc = dalloc(c, arr[a], N);
+            for (int a = 0; a < 6; ++a) *arr[a] = (double *)(base + a * part);
+            if (k.track_ids) c->ids[b] = (uint32_t *)(base + 6 * part);
         } else {
-            const int64_t part = align_up(N * 4, 256);
-            rc = dalloc(c, (char **)&c->p32_block[b], 8 * part);
-            if (rc == OHPIC_OK) {
-                char *base = (char *)c->p32_block[b];
-                c->p32[b].cell = (int32_t *)base;
-                float **arr[6] = {&c->p32[b].ox, &c->p32[b].oy, &c->p32[b].oz, &c->p32[b].vx, &c->p32[b].vy, &c->p32[b].vz};
-                for (int a = 0; a < 6; ++a) *arr[a] = (float *)(base + (a + 1) * part);
-                if (k.track_ids) c->ids[b] = (uint32_t *)(base + 7 * part);
-            }
+            c->p32[b].cell = (int32_t *)base;
+            float **arr[6] = {&c->p32[b].ox, &c->p32[b].oy, &c->p32[b].oz, &c->p32[b].vx, &c->p32[b].vy, &c->p32[b].vz};
+            for (int a = 0; a < 6; ++a) *arr[a] = (float *)(base + (a + 1) * part);
+            if (k.track_ids) c->ids[b] = (uint32_t *)(base + 7 * part);
         }
-        if (rc == OHPIC_OK && f64 && k.track_ids) rc = dalloc(c, &c->ids[b], N);
     }
     if (rc == OHPIC_OK) rc = dalloc(c, (char **)&c->rho, g.ncell * es);
     if (rc == OHPIC_OK && !f64) rc = dalloc(c, &c->wsum, (int64_t)k.nspecies * g.ncell);

@@ -199,9 +199,11 @@ struct ohpic_ctx {
     ohpic::PartF64 p64[2];
     ohpic::PartF32 p32[2];
     uint32_t *ids[2];
-    // FP32 form: each buffer is one allocation of eight word arrays (cell, offsets,
-    // velocities, ids), so it also holds N 32-byte sort records.
-    void *p32_block[2];
+    // Each particle buffer is one allocation of eight arrays, so it also holds N
+    // sort records: FP32 form eight 4-byte arrays (cell, offsets, velocities,
+    // ids) = 32-byte records; FP64 form eight 8-byte arrays (positions,
+    // velocities, ids, padding) = 64-byte records.
+    void *pblock[2];
     int cur;
 
     // fields

@@ -6,11 +6,12 @@
 //
 // Per species: histogram of cell keys (global atomics, aggregated per warp with
 // __match_any_sync), exclusive scan of the ncell counters (multi-level block
-// scan), tile start table, then a scatter of every particle into the second
-// buffer (FP32 form: as 32-byte records, transposed back into the first buffer's
-// word arrays by a sequential pass).  Lanes of a warp that share a key take
-// consecutive slots in lane order, so a warp's relative order is kept; order
-// across warps follows the atomic order.
+// scan), tile start table, then a scatter of every particle as one whole
+// record (32 bytes in the FP32 form, 64 in the FP64 form) into the second
+// buffer's block, transposed back into the first buffer's arrays by a
+// sequential pass.  Lanes of a warp that share a key take consecutive slots in
+// lane order, so a warp's relative order is kept; order across warps follows the
+// atomic order.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -112,21 +113,6 @@ __device__ __forceinline__ void rec_load(const PartF64 &s64, const PartF32 &s32,
 }
 
 template <bool F32>
-__device__ __forceinline__ void rec_store(const PartF64 &d64, const PartF32 &d32, uint32_t *did, int64_t j,
-                                          const Rec<F32> &r)
-{
-    if (F32) {
-        d32.cell[j] = r.cell;
-        d32.ox[j] = r.f[0]; d32.oy[j] = r.f[1]; d32.oz[j] = r.f[2];
-        d32.vx[j] = r.f[3]; d32.vy[j] = r.f[4]; d32.vz[j] = r.f[5];
-    } else {
-        d64.x[j] = r.a[0]; d64.y[j] = r.a[1]; d64.z[j] = r.a[2];
-        d64.vx[j] = r.a[3]; d64.vy[j] = r.a[4]; d64.vz[j] = r.a[5];
-    }
-    if (did) did[j] = r.id;
-}
-
-template <bool F32>
 __device__ __forceinline__ uint32_t rec_key(const Geom &g, const Rec<F32> &r, DevDiag *d)
 {
     int ix, iy, iz;
@@ -140,32 +126,6 @@ __device__ __forceinline__ uint32_t rec_key(const Geom &g, const Rec<F32> &r, De
         ix = iy = iz = 0;
     }
     return tile_key(g, ix, iy, iz);
-}
-
-template <bool F32>
-__global__ void k_scatter(Geom g, PartF64 s64, PartF32 s32, PartF64 d64, PartF32 d32, const uint32_t *sid,
-                          uint32_t *did, int64_t seg, int64_t n, const uint32_t *start, uint32_t *cursor, DevDiag *d)
-{
-    constexpr int U = 2;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += U * stride) {
-        Rec<F32> r[U];
-        bool act[U];
-        uint32_t key[U], slot[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int64_t i = base + u * stride + threadIdx.x;
-            act[u] = i < n;
-            if (act[u]) rec_load<F32>(s64, s32, sid, seg + i, r[u]);
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) key[u] = act[u] ? rec_key<F32>(g, r[u], d) : 0u;
-#pragma unroll
-        for (int u = 0; u < U; ++u) slot[u] = aggregated_inc(cursor, key[u], act[u]);
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-            if (act[u]) rec_store<F32>(d64, d32, did, seg + (int64_t)start[key[u]] + slot[u], r[u]);
-    }
 }
 
 // FP32 form: the scatter writes each particle as one 32-byte record (cell, three
@@ -217,6 +177,53 @@ __global__ void k_rec32_to_soa(const int4 *rec, int64_t seg, int64_t n, PartF32 
         p.ox[j] = __int_as_float(a.y); p.oy[j] = __int_as_float(a.z); p.oz[j] = __int_as_float(a.w);
         p.vx[j] = __int_as_float(b.x); p.vy[j] = __int_as_float(b.y); p.vz[j] = __int_as_float(b.z);
         if (ids) ids[j] = (uint32_t)b.w;
+    }
+}
+
+// FP64 form: one 64-byte record per particle (positions, velocities, id,
+// padding), two whole sectors, for the same reason.
+__device__ __forceinline__ void rec64_store(double2 *rec, int64_t j, const Rec<false> &r)
+{
+    rec[4 * j] = make_double2(r.a[0], r.a[1]);
+    rec[4 * j + 1] = make_double2(r.a[2], r.a[3]);
+    rec[4 * j + 2] = make_double2(r.a[4], r.a[5]);
+    rec[4 * j + 3] = make_double2(__longlong_as_double((long long)r.id), 0.0);
+}
+
+__global__ void k_scatter_rec64(Geom g, PartF64 s64, const uint32_t *sid, double2 *rec, int64_t seg, int64_t n,
+                                const uint32_t *start, uint32_t *cursor, DevDiag *d)
+{
+    constexpr int U = 2;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += U * stride) {
+        Rec<false> r[U];
+        bool act[U];
+        uint32_t key[U], slot[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t i = base + u * stride + threadIdx.x;
+            act[u] = i < n;
+            if (act[u]) rec_load<false>(s64, PartF32{}, sid, seg + i, r[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) key[u] = act[u] ? rec_key<false>(g, r[u], d) : 0u;
+#pragma unroll
+        for (int u = 0; u < U; ++u) slot[u] = aggregated_inc(cursor, key[u], act[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (act[u]) rec64_store(rec, seg + (int64_t)start[key[u]] + slot[u], r[u]);
+    }
+}
+
+__global__ void k_rec64_to_soa(const double2 *rec, int64_t seg, int64_t n, PartF64 p, uint32_t *ids)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int64_t j = seg + i;
+        const double2 a = rec[4 * j], b = rec[4 * j + 1], c = rec[4 * j + 2];
+        p.x[j] = a.x; p.y[j] = a.y; p.z[j] = b.x;
+        p.vx[j] = b.y; p.vy[j] = c.x; p.vz[j] = c.y;
+        if (ids) ids[j] = (uint32_t)__double_as_longlong(rec[4 * j + 3].x);
     }
 }
 
@@ -452,7 +459,7 @@ int sort_particles(ohpic_ctx *c)
 {
     const Geom &g = c->g;
     const bool f32 = c->cfg.precision == OHPIC_FP32;
-    const int src = c->cur, dst = 1 - c->cur;
+    const int src = c->cur, dst = 1 - c->cur;   // the records come back into the current buffer
     for (int s = 0; s < c->cfg.nspecies; ++s) {
         const int64_t n = c->count[s];
         int64_t *tb = c->tile_begin + (int64_t)s * (g.ntile + 1);
@@ -472,22 +479,21 @@ int sort_particles(ohpic_ctx *c)
         ++c->launches;
         if (n > 0) {
             cudaMemsetAsync(c->cell_count, 0, sizeof(uint32_t) * g.ncell, c->stream);
+            // records in the other buffer's block, then back into this buffer
             if (f32) {
-                // records in the other buffer's block, then back into this buffer
-                int4 *rec = (int4 *)c->p32_block[dst];
+                int4 *rec = (int4 *)c->pblock[dst];
                 k_scatter_rec32<<<grid_of(n), 256, 0, c->stream>>>(g, c->p32[src], c->ids[src], rec, c->seg[s], n,
                                                                    c->cell_start, c->cell_count, c->diag);
                 k_rec32_to_soa<<<grid_of(n), 256, 0, c->stream>>>(rec, c->seg[s], n, c->p32[src], c->ids[src]);
-                c->launches += 2;
             } else {
-                k_scatter<false><<<grid_of(n), 256, 0, c->stream>>>(g, c->p64[src], c->p32[src], c->p64[dst],
-                                                                    c->p32[dst], c->ids[src], c->ids[dst], c->seg[s],
-                                                                    n, c->cell_start, c->cell_count, c->diag);
-                ++c->launches;
+                double2 *rec = (double2 *)c->pblock[dst];
+                k_scatter_rec64<<<grid_of(n), 256, 0, c->stream>>>(g, c->p64[src], c->ids[src], rec, c->seg[s], n,
+                                                                   c->cell_start, c->cell_count, c->diag);
+                k_rec64_to_soa<<<grid_of(n), 256, 0, c->stream>>>(rec, c->seg[s], n, c->p64[src], c->ids[src]);
             }
+            c->launches += 2;
         }
     }
-    if (!f32) c->cur = dst;   // the FP32 records come back into the same buffer
     c->sorted = true;
     c->steps_since_sort = 0;
     return OHPIC_OK;
