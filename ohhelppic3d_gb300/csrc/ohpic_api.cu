@@ -42,7 +42,7 @@ namespace ohpic {
 
 // Grid geometry for a tile shape and halo; false when a tile edge is not a
 // divisor of the grid or the staged box does not fit one CTA's shared memory.
-bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g)
+bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g, int deposit_extra)
 {
     const int n[3] = {k.nx, k.ny, k.nz};
     for (int d = 0; d < 3; ++d)
@@ -59,10 +59,11 @@ bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g)
     g.tile_cells = g.tx * g.ty * g.tz;
     g.nxh = g.nx / 2 + 1;
     g.nspec = (int64_t)g.nxh * g.ny * g.nz;
-    // The FP32 deposit box reaches one cell further than the staged E box: at
-    // 8 bytes per node it is cheap, and it keeps the deposits of particles that
-    // drifted just outside the E box in shared memory.
-    g.dhalo = k.precision == OHPIC_FP64 ? halo : halo + 1;
+    // The FP32 deposit box may reach further than the staged E box: at 8 bytes
+    // per node it is cheap, and it keeps the deposits of particles that drifted
+    // just outside the E box in shared memory.
+    if (deposit_extra < 0 || deposit_extra > 2) return false;
+    g.dhalo = k.precision == OHPIC_FP64 ? halo : halo + deposit_extra;
     g.dsx = g.tx + 2 * g.dhalo + 1; g.dsy = g.ty + 2 * g.dhalo + 1; g.dsz = g.tz + 2 * g.dhalo + 1;
     // Staged E box (4 reals per node) plus the deposit box (8 bytes per node).
     const int64_t s3 = (int64_t)g.sx * g.sy * g.sz, s3d = (int64_t)g.dsx * g.dsy * g.dsz;

@@ -264,7 +264,8 @@ namespace ohpic {
 
 // Host helpers (ohpic_api.cu): geometry of a grid for a tile shape and halo
 // (false when it does not fit), and the FP64 Boris constants of one species.
-bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g);
+// deposit_extra: cells the FP32 deposit box reaches beyond the staged E box (0..2).
+bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g, int deposit_extra = 1);
 void species_consts(const ohpic_config &cfg, int s, double dt, SpeciesConst &k);
 
 // Kernel launchers: dispatch (convert.cu) and the two forms (push_f64.cu, push_f32.cu).

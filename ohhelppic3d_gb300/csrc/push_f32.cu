@@ -448,7 +448,7 @@ __device__ __forceinline__ int advance(const TileArgs &a, const Box &box, const 
 // One work item (a tile's particle range of one species) of one context.  smem
 // is the dynamic shared memory (E box, then the deposit box), ebar an mbarrier
 // for the TMA copy of the E box; emap may be null when a.use_tma is 0.
-template <int MODE, int DEP>
+template <int MODE, int DEP, bool kWide>
 __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap,
                                           const Item &it, unsigned char *smem, uint64_t *ebar)
 {
@@ -457,8 +457,9 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
     constexpr bool kDeposit = MODE == MODE_PUSH || MODE == MODE_DEPOSIT;
 
     const Geom &g = a.g;
-    const Box box = make_box(g, it), dbox = make_dbox(g, it);
-    const int s3 = g.sx * g.sy * g.sz, s3d = g.dsx * g.dsy * g.dsz;
+    // kWide: the deposit box may reach past the E box (else the geometry makes them equal)
+    const Box box = make_box(g, it), dbox = kWide ? make_dbox(g, it) : box;
+    const int s3 = g.sx * g.sy * g.sz, s3d = kWide ? g.dsx * g.dsy * g.dsz : s3;
     float4 *sE = (float4 *)smem;
     unsigned *slo = (unsigned *)(smem + (kGather ? (size_t)s3 * sizeof(float4) : 0));
     unsigned *shi = slo + s3d;
@@ -536,7 +537,7 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
 // the lanes' last sums once per 128 particles.  The per-particle arithmetic is
 // advance(), as in the two-per-lane pass, and every sum is integer, so both
 // passes give the same bits.
-template <int MODE, int DEP>
+template <int MODE, int DEP, bool kWide>
 __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap,
                                            const Item &it, unsigned char *smem, uint64_t *ebar)
 {
@@ -545,8 +546,9 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
     constexpr bool kMove = MODE == MODE_PUSH;
 
     const Geom &g = a.g;
-    const Box box = make_box(g, it), dbox = make_dbox(g, it);
-    const int s3 = g.sx * g.sy * g.sz, s3d = g.dsx * g.dsy * g.dsz;
+    // kWide: the deposit box may reach past the E box (else the geometry makes them equal)
+    const Box box = make_box(g, it), dbox = kWide ? make_dbox(g, it) : box;
+    const int s3 = g.sx * g.sy * g.sz, s3d = kWide ? g.dsx * g.dsy * g.dsz : s3;
     float4 *sE = (float4 *)smem;
     unsigned *slo = (unsigned *)(smem + (kGather ? (size_t)s3 * sizeof(float4) : 0));
     unsigned *shi = slo + s3d;
@@ -625,15 +627,18 @@ __device__ __forceinline__ unsigned char *align128(unsigned char *p)
 }
 
 // Work item b with PPL particles per lane: 2 (every mode) or 4 (push and deposit).
-template <int MODE, int DEP, int PPL>
+// kWide: whether the geometry's deposit box may be wider than its E box (the
+// single-context kernel; the multi-run kernel's geometries never are, and it
+// spends the registers elsewhere).
+template <int MODE, int DEP, int PPL, bool kWide>
 __device__ __forceinline__ void run_item(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap, int64_t b,
                                          unsigned char *smem, uint64_t *ebar)
 {
     Item it;
     if constexpr (PPL == 4) {
-        if (get_item<4>(a, b, it)) tile_pass4<MODE, DEP>(a, p, emap, it, smem, ebar);
+        if (get_item<4>(a, b, it)) tile_pass4<MODE, DEP, kWide>(a, p, emap, it, smem, ebar);
     } else {
-        if (get_item<2>(a, b, it)) tile_pass<MODE, DEP>(a, p, emap, it, smem, ebar);
+        if (get_item<2>(a, b, it)) tile_pass<MODE, DEP, kWide>(a, p, emap, it, smem, ebar);
     }
 }
 
@@ -644,7 +649,7 @@ __global__ void __launch_bounds__(256, 2) tiled_f32(TileArgs a, PartF32 p, const
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t ebar;
     // box start aligned to 128 bytes (the launch reserves the slack)
-    run_item<MODE, DEP, PPL>(a, p, &emap, (int64_t)blockIdx.x, align128(smem_raw), &ebar);
+    run_item<MODE, DEP, PPL, true>(a, p, &emap, (int64_t)blockIdx.x, align128(smem_raw), &ebar);
 }
 
 // Many contexts in one persistent launch.  Every CTA takes the next item from
@@ -696,7 +701,7 @@ __global__ void __launch_bounds__(256, 2) tiled_f32_multi(MultiPush m)
         // lands in local memory and costs 256 KB of local stores per item.
         const TileArgs &a = sd.a;
         const PartF32 &p = sd.p;
-        run_item<MODE, DEP, PPL>(a, p, nullptr, item - (r > 0 ? s_end[r - 1] : 0), smem, &ebar);
+        run_item<MODE, DEP, PPL, false>(a, p, nullptr, item - (r > 0 ? s_end[r - 1] : 0), smem, &ebar);
         __syncthreads();   // the next item reuses the shared boxes and descriptor
     }
 }

@@ -308,7 +308,9 @@ bool serve_geom(const ohpic_serve_config &cfg, int nx, int ny, int nz, Geom &g)
     tile_edges(cfg, t, tx);
     const int tile[3] = {pick_tile(nx, tx), pick_tile(ny, t), pick_tile(nz, t)};
     if (tile[0] < 1 || tile[1] < 1 || tile[2] < 1) return false;
-    return make_geom(k, tile, cfg.halo, g);
+    // served runs are short and sorted often, so their particles rarely drift past
+    // the E box: no extra deposit cells
+    return make_geom(k, tile, cfg.halo, g, 0);
 }
 
 // Allocation on the server's stream-ordered pool.
