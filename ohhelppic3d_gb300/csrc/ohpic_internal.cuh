@@ -195,7 +195,8 @@ struct ohpic_ctx {
     ohpic::SpeciesConst sc[OHPIC_MAX_SPECIES];
     double sc_dt;                       // dt the species constants were built for
 
-    // particle buffers: [0] current, [1] sort target
+    // particle buffers: [cur] holds the particles; the other one is the sort's
+    // record area (the sort works in place, so cur stays 0)
     ohpic::PartF64 p64[2];
     ohpic::PartF32 p32[2];
     uint32_t *ids[2];
