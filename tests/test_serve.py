@@ -165,6 +165,20 @@ def test_result_independent_of_sort_cadence_and_graphs(ohpic):
 
 
 @pytest.mark.gpu
+def test_result_independent_of_launch_shape(ohpic):
+    """Tile edges (cubic, or longer in x), deposit combination and particles per
+    lane change only how the work is cut: the integer deposit makes the state
+    bit-identical."""
+    P = ohpic
+    probe = _probe((32, 16, 16), 11, (42, 81))
+    ref, _ = _serve([probe])
+    for kw in ({"tile_x": 8}, {"tile": 4}, {"deposit": P.DEPOSIT_RUNS}, {"lane_particles": 2},
+               {"tile_x": 32, "halo": 2}):
+        got, _ = _serve([probe], **kw)
+        _same_state(ref[0], got[0])
+
+
+@pytest.mark.gpu
 def test_admission_by_hbm_budget(ohpic):
     from ohhelppic3d_gb300.serve import Server, thermal_request
     reqs = [thermal_request((32, 32, 32), 16, 15, seed=(42, 90 + i)) for i in range(6)]
