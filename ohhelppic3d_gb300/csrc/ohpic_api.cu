@@ -61,13 +61,21 @@ bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g, int 
     g.nspec = (int64_t)g.nxh * g.ny * g.nz;
     // The FP32 deposit box may reach further than the staged E box: at 8 bytes
     // per node it is cheap, and it keeps the deposits of particles that drifted
-    // just outside the E box in shared memory.
+    // just outside the E box in shared memory.  It widens only while the push
+    // CTA (boxes + prefetch stage) still fits two per SM.
     if (deposit_extra < 0 || deposit_extra > 2) return false;
-    g.dhalo = k.precision == OHPIC_FP64 ? halo : halo + deposit_extra;
-    g.dsx = g.tx + 2 * g.dhalo + 1; g.dsy = g.ty + 2 * g.dhalo + 1; g.dsz = g.tz + 2 * g.dhalo + 1;
-    // Staged E box (4 reals per node) plus the deposit box (8 bytes per node).
-    const int64_t s3 = (int64_t)g.sx * g.sy * g.sz, s3d = (int64_t)g.dsx * g.dsy * g.dsz;
+    const int64_t s3 = (int64_t)g.sx * g.sy * g.sz;
     const int64_t es = k.precision == OHPIC_FP64 ? 8 : 4;
+    if (k.precision == OHPIC_FP64) deposit_extra = 0;
+    for (;; --deposit_extra) {
+        g.dhalo = halo + deposit_extra;
+        g.dsx = g.tx + 2 * g.dhalo + 1; g.dsy = g.ty + 2 * g.dhalo + 1; g.dsz = g.tz + 2 * g.dhalo + 1;
+        const int64_t d3 = (int64_t)g.dsx * g.dsy * g.dsz;
+        const int64_t cta = ((s3 * 4 * es + d3 * 8 + 15) & ~(int64_t)15) + (int64_t)kQuadStageBytes + 128;
+        if (deposit_extra == 0 || cta <= (int64_t)kTwoCtaSmem) break;
+    }
+    // Staged E box (4 reals per node) plus the deposit box (8 bytes per node).
+    const int64_t s3d = (int64_t)g.dsx * g.dsy * g.dsz;
     // (leaves room for the FP32 push's 28 KB prefetch stage within a CTA's 227 KB)
     return s3 * 4 * es + s3d * 8 <= 192 * 1024;
 }

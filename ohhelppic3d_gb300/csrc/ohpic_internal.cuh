@@ -31,6 +31,11 @@ constexpr int kMaxHalo = 4;
 // FP32 push with four particles per lane: per-thread prefetch stage in shared memory
 // (7 arrays x 256 threads x 16 bytes).
 constexpr size_t kQuadStageBytes = 7 * 256 * 16;
+// Warps per CTA of the tile kernels (256 threads).
+constexpr int kTileWarps = 8;
+// Dynamic shared memory per FP32 push CTA that still lets two CTAs share an SM
+// (228 KB per SM, 1 KB reserved per CTA, under 1 KB of static shared memory).
+constexpr size_t kTwoCtaSmem = 112 * 1024;
 // FP32-form deposit: CIC weights in units of 2^-24 (the 8 weights of a particle sum to exactly 2^24).
 constexpr float kWeightScale = 16777216.0f;
 constexpr double kWeightUnit = 1.0 / 16777216.0;

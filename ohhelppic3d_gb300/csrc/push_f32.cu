@@ -714,6 +714,9 @@ static void launch_k(ohpic_ctx *c, void (*kernel)(TileArgs, P, const CUtensorMap
 {
     if (blocks <= 0) return;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // CTAs over ~96 KB pair up on an SM only with the whole shared-memory carveout
+    if (smem > 96 * 1024)
+        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     kernel<<<(unsigned)blocks, 256, smem, c->stream>>>(a, parts, c->emap);
     ++c->launches;
 }
