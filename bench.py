@@ -42,9 +42,9 @@ STEP_BYTES_PER_NODE = {"fp32": 72, "fp64": 144}
 # DRAM traffic of one push launch over its algorithmic bytes, from one ncu capture of
 # the push (dram__bytes_read.sum + dram__bytes_write.sum) at 128x128x64 with the same
 # tuned tile, halo and particle density (profiles/push_f32_128x128x64.md,
-# profiles/push_f64_128x128x64.md): 3.792 / 3.775 GB and 6.622 / 6.476 GB.  Both
+# profiles/push_f64_128x128x64.md): 3.799 / 3.775 GB and 6.622 / 6.476 GB.  Both
 # terms scale with the grid at fixed density, so the ratio carries to 256^3.
-PUSH_TRAFFIC_RATIO = {"fp32": 3.792314 / 3.774873600, "fp64": 6.621735 / 6.476005376}
+PUSH_TRAFFIC_RATIO = {"fp32": 3.799238 / 3.774873600, "fp64": 6.621735 / 6.476005376}
 
 
 def _peaks():
