@@ -237,6 +237,16 @@ struct SnapHeader {
 static_assert(sizeof(SnapHeader) == 256, "snapshot header is 256 bytes");
 
 // Bytes of one species' arrays: FP32 7 words + id; FP64 6 doubles + id, padded to 8.
+// A restored FP32 snapshot's cells must lie in the grid (the push relies on it).
+__global__ void k_check_cells(const int32_t *cell, int64_t n, int nx, int ny, int nz, DevDiag *d)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t c = cell[i];
+        if ((cell_x(c) >= nx || cell_y(c) >= ny || cell_z(c) >= nz) && atomicCAS(&d->err_code, 0, OHPIC_ERR_BOUNDS) == 0)
+            d->err_info = 11;
+    }
+}
+
 int64_t snap_species_bytes(bool f64, int64_t n)
 {
     return f64 ? (52 * n + 7) / 8 * 8 : 32 * n;
@@ -979,9 +989,22 @@ int ohpic_snapshot_load(ohpic_ctx *c, const void *host, int64_t bytes)
             OHPIC_CUDA_TRY(c, cudaMemcpyAsync(c->ids[c->cur] + c->seg[s], p + off, sizeof(uint32_t) * n,
                                               cudaMemcpyHostToDevice, c->stream));
         c->count[s] = n;
+        if (!f64 && n > 0) {
+            const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 16);
+            k_check_cells<<<(unsigned)blocks, 256, 0, c->stream>>>(c->p32[c->cur].cell + c->seg[s], n, c->cfg.nx,
+                                                                   c->cfg.ny, c->cfg.nz, c->diag);
+        }
         p += snap_species_bytes(f64, n);
     }
     OHPIC_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    {
+        const int rc = check_device(c);
+        if (rc != OHPIC_OK) {
+            // refuse the image and leave no particle that a kernel could misread
+            for (int s = 0; s < c->cfg.nspecies; ++s) c->count[s] = 0;
+            return fail(c, OHPIC_ERR_INVALID, "snapshot_load: a particle cell lies outside the grid");
+        }
+    }
     c->steps = h.steps;
     c->steps_since_sort = h.steps_since_sort;
     c->sorted = false;        // the next step sorts, then deposits the restored particles

@@ -370,11 +370,11 @@ __device__ __forceinline__ int advance(const TileArgs &a, const Box &box, const 
     constexpr bool kMove = MODE == MODE_PUSH || MODE == MODE_MOVE;
     constexpr bool kDeposit = MODE == MODE_PUSH || MODE == MODE_DEPOSIT;
     const Geom &g = a.g;
+    // Cells are valid by construction: uploads and the injector wrap positions
+    // into the grid (flagging anything else), the push wraps every cell it
+    // writes, and a restored snapshot is checked on load.  So no per-particle
+    // range check here (it cost 2.5% of the push).
     int ix = cell_x(s.cell), iy = cell_y(s.cell), iz = cell_z(s.cell);
-    if (ix >= g.nx || iy >= g.ny || iz >= g.nz) {
-        flag_error(a.diag, OHPIC_ERR_BOUNDS, 3);
-        return -1;
-    }
     if (kGather) {
         const int key = box.key(ix, iy, iz);
         t.out += key < 0;

@@ -4,7 +4,8 @@ A run interrupted after 7 steps and restarted from its snapshot in a fresh
 context must continue like the uninterrupted run: bit for bit in the FP32 form
 (its deposit is integer fixed point, so re-depositing the restored particles
 gives the same sums), within FP64 atomic rounding in the FP64 form.  Snapshots
-of another grid, truncated or foreign bytes are refused with a status code.
+of another grid, truncated or foreign bytes, and cells outside the grid are
+refused with a status code.
 """
 import numpy as np
 import pytest
@@ -77,5 +78,9 @@ def test_snapshot_mismatch_is_refused(ohpic):
         with P.PicContext(other) as b:
             with pytest.raises(P.OhpicError):
                 b.restore(snap)                              # another grid
+        bad = bytearray(snap)
+        bad[256:260] = b"\xff\xff\xff\xff"             # species 0, particle 0: cell out of the grid
+        with pytest.raises(P.OhpicError):
+            a.restore(bytes(bad))
         a.restore(snap)                                      # still usable
         a.step(0.1, 1)
