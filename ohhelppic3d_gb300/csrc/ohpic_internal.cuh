@@ -278,8 +278,8 @@ void species_consts(const ohpic_config &cfg, int s, double dt, SpeciesConst &k);
 void launch_tiled(ohpic_ctx *c, int mode, int strict);
 void launch_tiled_f64(ohpic_ctx *c, const TileArgs &a, int mode, int strict, int64_t blocks, size_t smem);
 void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks, size_t smem);
-cudaError_t launch_multi_f32(cudaStream_t st, int mode, int dep, int ppl, const MultiPush &m, int grid,
-                             size_t smem);
+cudaError_t launch_multi_f32(cudaStream_t st, int mode, int dep, int ppl, int weights, const MultiPush &m,
+                             int grid, size_t smem);
 void ensure_emap(ohpic_ctx *c);
 // Fields (fields.cu).
 int fields_setup(ohpic_ctx *c);

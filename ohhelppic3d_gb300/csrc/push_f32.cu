@@ -135,12 +135,13 @@ __device__ __forceinline__ void warp_run_deposit(int key, unsigned u[8], unsigne
 // rounded from its parent's FP32 product and clamped to the parent's integer, the
 // sibling is the difference, so every weight is non-negative and the eight add
 // up to 2^24 with no fix-up pass (7 float-to-integer conversions instead of 8).
-__device__ __forceinline__ void fixed_weights(int conv, float ox, float oy, float oz, unsigned u[8])
+template <int W>
+__device__ __forceinline__ void fixed_weights(float ox, float oy, float oz, unsigned u[8])
 {
     float wx0, wx1, wy0, wy1, wz0, wz1;
-    cic<float>(conv, ox, wx0, wx1);
-    cic<float>(conv, oy, wy0, wy1);
-    cic<float>(conv, oz, wz0, wz1);
+    cic_c<W, float>(ox, wx0, wx1);
+    cic_c<W, float>(oy, wy0, wy1);
+    cic_c<W, float>(oz, wz0, wz1);
     const float fx1 = wx1 * kWeightScale, fx0 = wx0 * kWeightScale;   // exact: power-of-two scale
     const unsigned X1 = __float2uint_rn(fx1), X0 = (1u << 24) - X1;
     const float f11 = fx1 * wy1, f01 = fx0 * wy1, f10 = fx1 * wy0, f00 = fx0 * wy0;
@@ -361,7 +362,7 @@ struct Tally {
 // the (new) position (PUSH/DEPOSIT).  Returns the box index of the deposit cell,
 // or -1 when there is no shared deposit (no deposit mode, outside the box: then
 // the weights already went to global memory, or an invalid cell).
-template <int MODE>
+template <int MODE, int W>
 __device__ __forceinline__ int advance(const TileArgs &a, const Box &box, const Box &dbox, bool e_ok,
                                        const float4 *sE, int sp,
                                        const Push32 &k, int64_t idx, P32 &s, unsigned u[8], Tally &t)
@@ -379,9 +380,9 @@ __device__ __forceinline__ int advance(const TileArgs &a, const Box &box, const 
         const int key = box.key(ix, iy, iz);
         t.out += key < 0;
         float wx0, wx1, wy0, wy1, wz0, wz1;
-        cic<float>(a.weights, s.ox, wx0, wx1);
-        cic<float>(a.weights, s.oy, wy0, wy1);
-        cic<float>(a.weights, s.oz, wz0, wz1);
+        cic_c<W, float>(s.ox, wx0, wx1);
+        cic_c<W, float>(s.oy, wy0, wy1);
+        cic_c<W, float>(s.oz, wz0, wz1);
         const float a00 = wx0 * wy0, a10 = wx1 * wy0, a01 = wx0 * wy1, a11 = wx1 * wy1;
         const float ww[8] = {a00 * wz0, a10 * wz0, a01 * wz0, a11 * wz0, a00 * wz1, a10 * wz1, a01 * wz1, a11 * wz1};
         float4 nd[8];
@@ -430,7 +431,7 @@ __device__ __forceinline__ int advance(const TileArgs &a, const Box &box, const 
         }
     }
     if (!kDeposit) return -1;
-    fixed_weights(a.weights, s.ox, s.oy, s.oz, u);
+    fixed_weights<W>(s.ox, s.oy, s.oz, u);
     const int dkey = dbox.key(ix, iy, iz);
     if (dkey < 0) {
         deposit_global_fixed(g, a.wsum + (int64_t)sp * g.ncell, ix, iy, iz, u);
@@ -448,7 +449,7 @@ __device__ __forceinline__ int advance(const TileArgs &a, const Box &box, const 
 // One work item (a tile's particle range of one species) of one context.  smem
 // is the dynamic shared memory (E box, then the deposit box), ebar an mbarrier
 // for the TMA copy of the E box; emap may be null when a.use_tma is 0.
-template <int MODE, int DEP, bool kWide>
+template <int MODE, int DEP, int W, bool kWide>
 __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap,
                                           const Item &it, unsigned char *smem, uint64_t *ebar)
 {
@@ -505,8 +506,8 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
 #pragma unroll
         for (int v = 0; v < 8; ++v) u0[v] = u1[v] = 0u;
         if (gv) {
-            if (2 * gi < end) k0 = advance<MODE>(a, box, dbox, e_ok, sE, sp, k, 2 * gi, cur[0], u0, t);
-            if (2 * gi + 1 < end) k1 = advance<MODE>(a, box, dbox, e_ok, sE, sp, k, 2 * gi + 1, cur[1], u1, t);
+            if (2 * gi < end) k0 = advance<MODE, W>(a, box, dbox, e_ok, sE, sp, k, 2 * gi, cur[0], u0, t);
+            if (2 * gi + 1 < end) k1 = advance<MODE, W>(a, box, dbox, e_ok, sE, sp, k, 2 * gi + 1, cur[1], u1, t);
             if (kMove) store_pair(p, gi, cur);
         }
         if (kDeposit) {
@@ -537,7 +538,7 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
 // the lanes' last sums once per 128 particles.  The per-particle arithmetic is
 // advance(), as in the two-per-lane pass, and every sum is integer, so both
 // passes give the same bits.
-template <int MODE, int DEP, bool kWide>
+template <int MODE, int DEP, int W, bool kWide>
 __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap,
                                            const Item &it, unsigned char *smem, uint64_t *ebar)
 {
@@ -596,7 +597,7 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
             for (int j = 0; j < 4; ++j) {
                 if (4 * gi + j < end) {
                     unsigned u[8];
-                    const int kk = advance<MODE>(a, box, dbox, e_ok, sE, sp, k, 4 * gi + j, q[j], u, t);
+                    const int kk = advance<MODE, W>(a, box, dbox, e_ok, sE, sp, k, 4 * gi + j, q[j], u, t);
                     if (kk >= 0) {
                         if (kk != acc_key) {
                             if (acc_key >= 0) box_add8(shi, slo, acc_key, dbox.sx, dbox.sxy, acc);
@@ -630,26 +631,26 @@ __device__ __forceinline__ unsigned char *align128(unsigned char *p)
 // kWide: whether the geometry's deposit box may be wider than its E box (the
 // single-context kernel; the multi-run kernel's geometries never are, and it
 // spends the registers elsewhere).
-template <int MODE, int DEP, int PPL, bool kWide>
+template <int MODE, int DEP, int PPL, int W, bool kWide>
 __device__ __forceinline__ void run_item(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap, int64_t b,
                                          unsigned char *smem, uint64_t *ebar)
 {
     Item it;
     if constexpr (PPL == 4) {
-        if (get_item<4>(a, b, it)) tile_pass4<MODE, DEP, kWide>(a, p, emap, it, smem, ebar);
+        if (get_item<4>(a, b, it)) tile_pass4<MODE, DEP, W, kWide>(a, p, emap, it, smem, ebar);
     } else {
-        if (get_item<2>(a, b, it)) tile_pass<MODE, DEP, kWide>(a, p, emap, it, smem, ebar);
+        if (get_item<2>(a, b, it)) tile_pass<MODE, DEP, W, kWide>(a, p, emap, it, smem, ebar);
     }
 }
 
 // One context: one CTA per work item.
-template <int MODE, int DEP, int PPL>
+template <int MODE, int DEP, int PPL, int W>
 __global__ void __launch_bounds__(256, 2) tiled_f32(TileArgs a, PartF32 p, const __grid_constant__ CUtensorMap emap)
 {
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t ebar;
     // box start aligned to 128 bytes (the launch reserves the slack)
-    run_item<MODE, DEP, PPL, true>(a, p, &emap, (int64_t)blockIdx.x, align128(smem_raw), &ebar);
+    run_item<MODE, DEP, PPL, W, true>(a, p, &emap, (int64_t)blockIdx.x, align128(smem_raw), &ebar);
 }
 
 // Many contexts in one persistent launch.  Every CTA takes the next item from
@@ -658,7 +659,7 @@ __global__ void __launch_bounds__(256, 2) tiled_f32(TileArgs a, PartF32 p, const
 // shared memory when the run changes, and runs the same tile pass.  Runs are
 // ordered by decreasing particles per item, so the queue hands out the long
 // items first.
-template <int MODE, int DEP, int PPL>
+template <int MODE, int DEP, int PPL, int W>
 __global__ void __launch_bounds__(256, 2) tiled_f32_multi(MultiPush m)
 {
     extern __shared__ unsigned char smem_raw[];
@@ -701,7 +702,7 @@ __global__ void __launch_bounds__(256, 2) tiled_f32_multi(MultiPush m)
         // lands in local memory and costs 256 KB of local stores per item.
         const TileArgs &a = sd.a;
         const PartF32 &p = sd.p;
-        run_item<MODE, DEP, PPL, false>(a, p, nullptr, item - (r > 0 ? s_end[r - 1] : 0), smem, &ebar);
+        run_item<MODE, DEP, PPL, W, false>(a, p, nullptr, item - (r > 0 ? s_end[r - 1] : 0), smem, &ebar);
         __syncthreads();   // the next item reuses the shared boxes and descriptor
     }
 }
@@ -742,29 +743,40 @@ static auto by_lanes(int ppl, F f)
     return f(std::integral_constant<int, 2>());
 }
 
+template <typename F>
+static auto by_weights(int w, F f)
+{
+    if (w == OHPIC_WEIGHTS_REFERENCE) return f(std::integral_constant<int, OHPIC_WEIGHTS_REFERENCE>());
+    return f(std::integral_constant<int, OHPIC_WEIGHTS_STANDARD>());
+}
+
 void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks, size_t smem)
 {
     const PartF32 &pp = c->p32[c->cur];
-    if (mode == MODE_PUSH || mode == MODE_DEPOSIT) {
-        by_lanes(a.ppl, [&](auto l) {
-            return by_deposit(a.deposit, [&](auto d) {
-                constexpr int D = decltype(d)::value, L = decltype(l)::value;
-                if (mode == MODE_PUSH) launch_k(c, tiled_f32<MODE_PUSH, D, L>, a, blocks, smem, pp);
-                else launch_k(c, tiled_f32<MODE_DEPOSIT, D, L>, a, blocks, smem, pp);
-                return 0;
+    by_weights(a.weights, [&](auto w) {
+        constexpr int W = decltype(w)::value;
+        if (mode == MODE_PUSH || mode == MODE_DEPOSIT) {
+            by_lanes(a.ppl, [&](auto l) {
+                return by_deposit(a.deposit, [&](auto d) {
+                    constexpr int D = decltype(d)::value, L = decltype(l)::value;
+                    if (mode == MODE_PUSH) launch_k(c, tiled_f32<MODE_PUSH, D, L, W>, a, blocks, smem, pp);
+                    else launch_k(c, tiled_f32<MODE_DEPOSIT, D, L, W>, a, blocks, smem, pp);
+                    return 0;
+                });
             });
-        });
-    } else if (mode == MODE_MOVE) {
-        launch_k(c, tiled_f32<MODE_MOVE, OHPIC_DEPOSIT_RUNS, 2>, a, blocks, smem, pp);
-    } else {
-        launch_k(c, tiled_f32<MODE_INTERP, OHPIC_DEPOSIT_RUNS, 2>, a, blocks, smem, pp);
-    }
+        } else if (mode == MODE_MOVE) {
+            launch_k(c, tiled_f32<MODE_MOVE, OHPIC_DEPOSIT_RUNS, 2, W>, a, blocks, smem, pp);
+        } else {
+            launch_k(c, tiled_f32<MODE_INTERP, OHPIC_DEPOSIT_RUNS, 2, W>, a, blocks, smem, pp);
+        }
+        return 0;
+    });
 }
 
-template <int MODE, int DEP, int PPL>
+template <int MODE, int DEP, int PPL, int W>
 static cudaError_t launch_multi_k(cudaStream_t st, const MultiPush &m, int grid, size_t smem)
 {
-    auto kernel = tiled_f32_multi<MODE, DEP, PPL>;
+    auto kernel = tiled_f32_multi<MODE, DEP, PPL, W>;
     cudaError_t e = cudaSuccess;
     if (smem > 48 * 1024) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -772,15 +784,17 @@ static cudaError_t launch_multi_k(cudaStream_t st, const MultiPush &m, int grid,
     return cudaGetLastError();
 }
 
-cudaError_t launch_multi_f32(cudaStream_t st, int mode, int dep, int ppl, const MultiPush &m, int grid,
-                             size_t smem)
+cudaError_t launch_multi_f32(cudaStream_t st, int mode, int dep, int ppl, int weights, const MultiPush &m,
+                             int grid, size_t smem)
 {
     if (grid <= 0) return cudaSuccess;
-    return by_lanes(ppl, [&](auto l) {
-        return by_deposit(dep, [&](auto d) {
-            constexpr int D = decltype(d)::value, L = decltype(l)::value;
-            if (mode == MODE_DEPOSIT) return launch_multi_k<MODE_DEPOSIT, D, L>(st, m, grid, smem);
-            return launch_multi_k<MODE_PUSH, D, L>(st, m, grid, smem);
+    return by_weights(weights, [&](auto w) {
+        return by_lanes(ppl, [&](auto l) {
+            return by_deposit(dep, [&](auto d) {
+                constexpr int D = decltype(d)::value, L = decltype(l)::value, W = decltype(w)::value;
+                if (mode == MODE_DEPOSIT) return launch_multi_k<MODE_DEPOSIT, D, L, W>(st, m, grid, smem);
+                return launch_multi_k<MODE_PUSH, D, L, W>(st, m, grid, smem);
+            });
         });
     });
 }

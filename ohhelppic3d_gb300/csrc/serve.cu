@@ -628,7 +628,8 @@ int64_t enqueue_step(Server *s, int mode)
         }
     }
     cudaMemsetAsync(s->d_cursor, 0, sizeof(unsigned long long), s->st);
-    if (launch_multi_f32(s->st, mode, s->cfg.deposit, s->cfg.lane_particles, multi_push(s), s->push_grid,
+    if (launch_multi_f32(s->st, mode, s->cfg.deposit, s->cfg.lane_particles, s->cfg.weights, multi_push(s),
+                         s->push_grid,
                          s->push_smem) != cudaSuccess)
         return -1;
     return l + 2;

@@ -51,6 +51,20 @@ __device__ __forceinline__ void cic(int conv, T r, T &w0, T &w1)
     }
 }
 
+// The same with the convention fixed at compile time (the FP32 kernels are
+// instantiated per convention: a run-time choice cost two selects per axis).
+template <int CONV, typename T>
+__device__ __forceinline__ void cic_c(T r, T &w0, T &w1)
+{
+    if (CONV == OHPIC_WEIGHTS_REFERENCE) {
+        w0 = r;
+        w1 = T(1) - r;
+    } else {
+        w0 = T(1) - r;
+        w1 = r;
+    }
+}
+
 __device__ __forceinline__ int wrapi(int i, int n)
 {
     i %= n;
