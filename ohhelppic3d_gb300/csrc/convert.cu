@@ -240,7 +240,7 @@ void launch_tiled(ohpic_ctx *c, int mode, int strict)
             blocks += (groups * PPT + a.chunk - 1) / a.chunk;
         }
     }
-    const int64_t s3 = (int64_t)c->g.sx * c->g.sy * c->g.sz, s3d = (int64_t)c->g.dsx * c->g.dsy * c->g.dsz;
+    const int64_t s3 = (int64_t)c->g.sx * c->g.sy * c->g.sz;
     const size_t es = f64 ? 8 : 4;
     const bool gather = mode != MODE_DEPOSIT;
     const bool dep = mode == MODE_PUSH || mode == MODE_DEPOSIT;
@@ -248,10 +248,10 @@ void launch_tiled(ohpic_ctx *c, int mode, int strict)
     // E box: 4 reals per node; deposit box: one real per node (FP64) or the
     // low and high 32-bit words of the fixed-point sums (FP32).
     // (+128: the kernels align the box start to 128 bytes for TMA)
-    if (a.sorted) smem = (gather ? s3 * 4 * es : 0) + (dep ? s3d * 8 : 0) + 128;
+    if (a.sorted) smem = (gather ? s3 * 4 * es : 0) + (dep ? s3 * 8 : 0) + 128;
     // four per lane (FP32 push/deposit): the boxes end on a 16-byte boundary and are
     // followed by the per-thread prefetch stage (7 arrays x 256 threads x 16 bytes)
-    if (!f64 && a.ppl == 4) smem = (a.sorted ? ((s3 * 4 * es + s3d * 8 + 15) & ~(size_t)15) : 0) + kQuadStageBytes + 128;
+    if (!f64 && a.ppl == 4) smem = (a.sorted ? ((s3 * 4 * es + s3 * 8 + 15) & ~(size_t)15) : 0) + kQuadStageBytes + 128;
     if (f64)
         launch_tiled_f64(c, a, mode, strict, blocks, smem);
     else

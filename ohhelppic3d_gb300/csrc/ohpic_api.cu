@@ -42,7 +42,7 @@ namespace ohpic {
 
 // Grid geometry for a tile shape and halo; false when a tile edge is not a
 // divisor of the grid or the staged box does not fit one CTA's shared memory.
-bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g, int deposit_extra)
+bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g)
 {
     const int n[3] = {k.nx, k.ny, k.nz};
     for (int d = 0; d < 3; ++d)
@@ -59,25 +59,11 @@ bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g, int 
     g.tile_cells = g.tx * g.ty * g.tz;
     g.nxh = g.nx / 2 + 1;
     g.nspec = (int64_t)g.nxh * g.ny * g.nz;
-    // The FP32 deposit box may reach further than the staged E box: at 8 bytes
-    // per node it is cheap, and it keeps the deposits of particles that drifted
-    // just outside the E box in shared memory.  It widens only while the push
-    // CTA (boxes + prefetch stage) still fits two per SM.
-    if (deposit_extra < 0 || deposit_extra > 2) return false;
+    // Staged E box (4 reals per node) plus the deposit box (8 bytes per node).
     const int64_t s3 = (int64_t)g.sx * g.sy * g.sz;
     const int64_t es = k.precision == OHPIC_FP64 ? 8 : 4;
-    if (k.precision == OHPIC_FP64) deposit_extra = 0;
-    for (;; --deposit_extra) {
-        g.dhalo = halo + deposit_extra;
-        g.dsx = g.tx + 2 * g.dhalo + 1; g.dsy = g.ty + 2 * g.dhalo + 1; g.dsz = g.tz + 2 * g.dhalo + 1;
-        const int64_t d3 = (int64_t)g.dsx * g.dsy * g.dsz;
-        const int64_t cta = ((s3 * 4 * es + d3 * 8 + 15) & ~(int64_t)15) + (int64_t)kQuadStageBytes + 128;
-        if (deposit_extra == 0 || cta <= (int64_t)kTwoCtaSmem) break;
-    }
-    // Staged E box (4 reals per node) plus the deposit box (8 bytes per node).
-    const int64_t s3d = (int64_t)g.dsx * g.dsy * g.dsz;
     // (leaves room for the FP32 push's 28 KB prefetch stage within a CTA's 227 KB)
-    return s3 * 4 * es + s3d * 8 <= 192 * 1024;
+    return s3 * (4 * es + 8) <= 192 * 1024;
 }
 
 // Boris constants of one species for a time step (particle_mover_boris.f90:37-43),

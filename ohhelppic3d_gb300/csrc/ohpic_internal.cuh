@@ -33,9 +33,6 @@ constexpr int kMaxHalo = 4;
 constexpr size_t kQuadStageBytes = 7 * 256 * 16;
 // Warps per CTA of the tile kernels (256 threads).
 constexpr int kTileWarps = 8;
-// Dynamic shared memory per FP32 push CTA that still lets two CTAs share an SM
-// (228 KB per SM, 1 KB reserved per CTA, under 1 KB of static shared memory).
-constexpr size_t kTwoCtaSmem = 112 * 1024;
 // FP32-form deposit: CIC weights in units of 2^-24 (the 8 weights of a particle sum to exactly 2^24).
 constexpr float kWeightScale = 16777216.0f;
 constexpr double kWeightUnit = 1.0 / 16777216.0;
@@ -60,8 +57,6 @@ struct Geom {
     int ntx, nty, ntz;     // tiles per axis
     int halo;              // cells staged around a tile
     int sx, sy, sz;        // staged nodes per axis: t + 2*halo + 1
-    int dhalo;             // cells of the deposit box around a tile (FP32 form: halo + 1)
-    int dsx, dsy, dsz;     // deposit box nodes per axis: t + 2*dhalo + 1
     int gx, gy, gz;        // padded E nodes per axis: n + 2*halo + 1
     int64_t ncell;
     int64_t ntile;
@@ -270,8 +265,7 @@ namespace ohpic {
 
 // Host helpers (ohpic_api.cu): geometry of a grid for a tile shape and halo
 // (false when it does not fit), and the FP64 Boris constants of one species.
-// deposit_extra: cells the FP32 deposit box reaches beyond the staged E box (0..2).
-bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g, int deposit_extra = 1);
+bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g);
 void species_consts(const ohpic_config &cfg, int s, double dt, SpeciesConst &k);
 
 // Kernel launchers: dispatch (convert.cu) and the two forms (push_f64.cu, push_f32.cu).

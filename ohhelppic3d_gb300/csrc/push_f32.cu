@@ -189,8 +189,8 @@ __device__ __forceinline__ void stage_f32(const TileArgs &a, const Item &it, flo
         }
     }
     if (need_w) {
-        const int s3d = g.dsx * g.dsy * g.dsz;
-        for (int i = threadIdx.x; i < s3d; i += blockDim.x) {
+        const int s3 = g.sx * g.sy * g.sz;
+        for (int i = threadIdx.x; i < s3; i += blockDim.x) {
             lo[i] = 0u;
             hi[i] = 0u;
         }
@@ -201,17 +201,17 @@ __device__ __forceinline__ void flush_f32(const TileArgs &a, const Item &it, con
 {
     const Geom &g = a.g;
     unsigned long long *w = a.wsum + (int64_t)it.sp * g.ncell;
-    const int rows = g.dsy * g.dsz, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int rows = g.sy * g.sz, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int r = threadIdx.x >> 5; r < rows; r += nw) {
-        const int cz = r / g.dsy, by = r - cz * g.dsy;
-        const int y = wrapi(it.y0 - g.dhalo + by, g.ny);
-        const int z = wrapi(it.z0 - g.dhalo + cz, g.nz);
+        const int cz = r / g.sy, by = r - cz * g.sy;
+        const int y = wrapi(it.y0 - g.halo + by, g.ny);
+        const int z = wrapi(it.z0 - g.halo + cz, g.nz);
         unsigned long long *row = w + (int64_t)g.nx * (y + (int64_t)g.ny * z);
-        const int base = r * g.dsx;
-        for (int ax = lane; ax < g.dsx; ax += 32) {
+        const int base = r * g.sx;
+        for (int ax = lane; ax < g.sx; ax += 32) {
             const unsigned long long v = ((unsigned long long)hi[base + ax] << 32) | lo[base + ax];
             if (v) {
-                int x = it.x0 - g.dhalo + ax;
+                int x = it.x0 - g.halo + ax;
                 if ((unsigned)x >= (unsigned)g.nx) x = wrapi(x, g.nx);
                 atomicAdd(row + x, v);
             }
@@ -363,8 +363,7 @@ struct Tally {
 // or -1 when there is no shared deposit (no deposit mode, outside the box: then
 // the weights already went to global memory, or an invalid cell).
 template <int MODE, int W>
-__device__ __forceinline__ int advance(const TileArgs &a, const Box &box, const Box &dbox, bool e_ok,
-                                       const float4 *sE, int sp,
+__device__ __forceinline__ int advance(const TileArgs &a, const Box &box, bool e_ok, const float4 *sE, int sp,
                                        const Push32 &k, int64_t idx, P32 &s, unsigned u[8], Tally &t)
 {
     constexpr bool kGather = MODE != MODE_DEPOSIT;
@@ -432,7 +431,7 @@ __device__ __forceinline__ int advance(const TileArgs &a, const Box &box, const 
     }
     if (!kDeposit) return -1;
     fixed_weights<W>(s.ox, s.oy, s.oz, u);
-    const int dkey = dbox.key(ix, iy, iz);
+    const int dkey = box.key(ix, iy, iz);
     if (dkey < 0) {
         deposit_global_fixed(g, a.wsum + (int64_t)sp * g.ncell, ix, iy, iz, u);
         if (!kGather) ++t.out;
@@ -449,7 +448,7 @@ __device__ __forceinline__ int advance(const TileArgs &a, const Box &box, const 
 // One work item (a tile's particle range of one species) of one context.  smem
 // is the dynamic shared memory (E box, then the deposit box), ebar an mbarrier
 // for the TMA copy of the E box; emap may be null when a.use_tma is 0.
-template <int MODE, int DEP, int W, bool kWide>
+template <int MODE, int DEP, int W>
 __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap,
                                           const Item &it, unsigned char *smem, uint64_t *ebar)
 {
@@ -458,12 +457,11 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
     constexpr bool kDeposit = MODE == MODE_PUSH || MODE == MODE_DEPOSIT;
 
     const Geom &g = a.g;
-    // kWide: the deposit box may reach past the E box (else the geometry makes them equal)
-    const Box box = make_box(g, it), dbox = kWide ? make_dbox(g, it) : box;
-    const int s3 = g.sx * g.sy * g.sz, s3d = kWide ? g.dsx * g.dsy * g.dsz : s3;
+    const Box box = make_box(g, it);
+    const int s3 = g.sx * g.sy * g.sz;
     float4 *sE = (float4 *)smem;
     unsigned *slo = (unsigned *)(smem + (kGather ? (size_t)s3 * sizeof(float4) : 0));
-    unsigned *shi = slo + s3d;
+    unsigned *shi = slo + s3;
     // The E box arrives by one TMA copy while the threads clear the deposit box.
     const bool tma = box.on && kGather && a.use_tma && emap != nullptr;
     if (tma && threadIdx.x == 0) {
@@ -506,8 +504,8 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
 #pragma unroll
         for (int v = 0; v < 8; ++v) u0[v] = u1[v] = 0u;
         if (gv) {
-            if (2 * gi < end) k0 = advance<MODE, W>(a, box, dbox, e_ok, sE, sp, k, 2 * gi, cur[0], u0, t);
-            if (2 * gi + 1 < end) k1 = advance<MODE, W>(a, box, dbox, e_ok, sE, sp, k, 2 * gi + 1, cur[1], u1, t);
+            if (2 * gi < end) k0 = advance<MODE, W>(a, box, e_ok, sE, sp, k, 2 * gi, cur[0], u0, t);
+            if (2 * gi + 1 < end) k1 = advance<MODE, W>(a, box, e_ok, sE, sp, k, 2 * gi + 1, cur[1], u1, t);
             if (kMove) store_pair(p, gi, cur);
         }
         if (kDeposit) {
@@ -516,8 +514,8 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
                 for (int v = 0; v < 8; ++v) u0[v] += u1[v];
                 k1 = -1;
             }
-            warp_run_deposit<DEP>(k0, u0, slo, shi, dbox.sx, dbox.sxy);
-            if (__any_sync(kFull, k1 >= 0)) warp_run_deposit<DEP>(k1, u1, slo, shi, dbox.sx, dbox.sxy);
+            warp_run_deposit<DEP>(k0, u0, slo, shi, box.sx, box.sxy);
+            if (__any_sync(kFull, k1 >= 0)) warp_run_deposit<DEP>(k1, u1, slo, shi, box.sx, box.sxy);
         }
         gi = gn;
         gv = vn;
@@ -538,7 +536,7 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
 // the lanes' last sums once per 128 particles.  The per-particle arithmetic is
 // advance(), as in the two-per-lane pass, and every sum is integer, so both
 // passes give the same bits.
-template <int MODE, int DEP, int W, bool kWide>
+template <int MODE, int DEP, int W>
 __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap,
                                            const Item &it, unsigned char *smem, uint64_t *ebar)
 {
@@ -547,12 +545,11 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
     constexpr bool kMove = MODE == MODE_PUSH;
 
     const Geom &g = a.g;
-    // kWide: the deposit box may reach past the E box (else the geometry makes them equal)
-    const Box box = make_box(g, it), dbox = kWide ? make_dbox(g, it) : box;
-    const int s3 = g.sx * g.sy * g.sz, s3d = kWide ? g.dsx * g.dsy * g.dsz : s3;
+    const Box box = make_box(g, it);
+    const int s3 = g.sx * g.sy * g.sz;
     float4 *sE = (float4 *)smem;
     unsigned *slo = (unsigned *)(smem + (kGather ? (size_t)s3 * sizeof(float4) : 0));
-    unsigned *shi = slo + s3d;
+    unsigned *shi = slo + s3;
     const bool tma = box.on && kGather && a.use_tma && emap != nullptr;
     if (tma && threadIdx.x == 0) {
         mbar_init(ebar, 1);
@@ -579,7 +576,7 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
     const int64_t end = a.seg[sp] + a.count[sp];
     Tally t;
     // Prefetch stage after the boxes (16-byte aligned); the launch reserves it.
-    const size_t boxes = box.on ? ((kGather ? (size_t)s3 * sizeof(float4) : 0) + (size_t)s3d * 8 + 15) & ~(size_t)15 : 0;
+    const size_t boxes = box.on ? ((kGather ? (size_t)s3 * sizeof(float4) : 0) + (size_t)s3 * 8 + 15) & ~(size_t)15 : 0;
     float4 *stage = (float4 *)(smem + boxes);
     if (it.g0 + threadIdx.x < it.g1) prefetch_quad<kGather>(stage, p, it.g0 + threadIdx.x);
 
@@ -597,10 +594,10 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
             for (int j = 0; j < 4; ++j) {
                 if (4 * gi + j < end) {
                     unsigned u[8];
-                    const int kk = advance<MODE, W>(a, box, dbox, e_ok, sE, sp, k, 4 * gi + j, q[j], u, t);
+                    const int kk = advance<MODE, W>(a, box, e_ok, sE, sp, k, 4 * gi + j, q[j], u, t);
                     if (kk >= 0) {
                         if (kk != acc_key) {
-                            if (acc_key >= 0) box_add8(shi, slo, acc_key, dbox.sx, dbox.sxy, acc);
+                            if (acc_key >= 0) box_add8(shi, slo, acc_key, box.sx, box.sxy, acc);
                             acc_key = kk;
 #pragma unroll
                             for (int v = 0; v < 8; ++v) acc[v] = u[v];
@@ -613,7 +610,7 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
             }
             if (kMove) store_quad(p, gi, q);
         }
-        warp_run_deposit<DEP>(acc_key, acc, slo, shi, dbox.sx, dbox.sxy);
+        warp_run_deposit<DEP>(acc_key, acc, slo, shi, box.sx, box.sxy);
     }
     if (box.on) {
         __syncthreads();
@@ -628,18 +625,15 @@ __device__ __forceinline__ unsigned char *align128(unsigned char *p)
 }
 
 // Work item b with PPL particles per lane: 2 (every mode) or 4 (push and deposit).
-// kWide: whether the geometry's deposit box may be wider than its E box (the
-// single-context kernel; the multi-run kernel's geometries never are, and it
-// spends the registers elsewhere).
-template <int MODE, int DEP, int PPL, int W, bool kWide>
+template <int MODE, int DEP, int PPL, int W>
 __device__ __forceinline__ void run_item(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap, int64_t b,
                                          unsigned char *smem, uint64_t *ebar)
 {
     Item it;
     if constexpr (PPL == 4) {
-        if (get_item<4>(a, b, it)) tile_pass4<MODE, DEP, W, kWide>(a, p, emap, it, smem, ebar);
+        if (get_item<4>(a, b, it)) tile_pass4<MODE, DEP, W>(a, p, emap, it, smem, ebar);
     } else {
-        if (get_item<2>(a, b, it)) tile_pass<MODE, DEP, W, kWide>(a, p, emap, it, smem, ebar);
+        if (get_item<2>(a, b, it)) tile_pass<MODE, DEP, W>(a, p, emap, it, smem, ebar);
     }
 }
 
@@ -650,7 +644,7 @@ __global__ void __launch_bounds__(256, 2) tiled_f32(TileArgs a, PartF32 p, const
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t ebar;
     // box start aligned to 128 bytes (the launch reserves the slack)
-    run_item<MODE, DEP, PPL, W, true>(a, p, &emap, (int64_t)blockIdx.x, align128(smem_raw), &ebar);
+    run_item<MODE, DEP, PPL, W>(a, p, &emap, (int64_t)blockIdx.x, align128(smem_raw), &ebar);
 }
 
 // Many contexts in one persistent launch.  Every CTA takes the next item from
@@ -702,7 +696,7 @@ __global__ void __launch_bounds__(256, 2) tiled_f32_multi(MultiPush m)
         // lands in local memory and costs 256 KB of local stores per item.
         const TileArgs &a = sd.a;
         const PartF32 &p = sd.p;
-        run_item<MODE, DEP, PPL, W, false>(a, p, nullptr, item - (r > 0 ? s_end[r - 1] : 0), smem, &ebar);
+        run_item<MODE, DEP, PPL, W>(a, p, nullptr, item - (r > 0 ? s_end[r - 1] : 0), smem, &ebar);
         __syncthreads();   // the next item reuses the shared boxes and descriptor
     }
 }

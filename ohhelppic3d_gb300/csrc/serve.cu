@@ -308,9 +308,7 @@ bool serve_geom(const ohpic_serve_config &cfg, int nx, int ny, int nz, Geom &g)
     tile_edges(cfg, t, tx);
     const int tile[3] = {pick_tile(nx, tx), pick_tile(ny, t), pick_tile(nz, t)};
     if (tile[0] < 1 || tile[1] < 1 || tile[2] < 1) return false;
-    // served runs are short and sorted often, so their particles rarely drift past
-    // the E box: no extra deposit cells
-    return make_geom(k, tile, cfg.halo, g, 0);
+    return make_geom(k, tile, cfg.halo, g);
 }
 
 // Allocation on the server's stream-ordered pool.
@@ -567,8 +565,7 @@ void fixed_shapes(Server *s)
     tile_edges(s->cfg, t, tx);
     const int n = 2 * std::max(t, tx);   // the largest staged box any grid gets
     serve_geom(s->cfg, n, n, n, g);
-    s->push_smem = (size_t)((((int64_t)g.sx * g.sy * g.sz * 16 + (int64_t)g.dsx * g.dsy * g.dsz * 8 + 15) &
-                             ~(int64_t)15) + 128 +
+    s->push_smem = (size_t)((((int64_t)g.sx * g.sy * g.sz * (16 + 8) + 15) & ~(int64_t)15) + 128 +
                             (s->cfg.lane_particles == 4 ? kQuadStageBytes : 0));
     s->push_grid = s->sms * 2;
     int64_t nt = 0;

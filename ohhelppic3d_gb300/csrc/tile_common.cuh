@@ -183,22 +183,6 @@ struct Box {
     }
 };
 
-// The deposit box: the same, with the deposit halo (FP32 form: one cell wider).
-__device__ __forceinline__ Box make_dbox(const Geom &g, const Item &it)
-{
-    Box b;
-    b.ox = it.x0 - g.dhalo;
-    b.oy = it.y0 - g.dhalo;
-    b.oz = it.z0 - g.dhalo;
-    b.spx = (unsigned)(g.tx + 2 * g.dhalo);
-    b.spy = (unsigned)(g.ty + 2 * g.dhalo);
-    b.spz = (unsigned)(g.tz + 2 * g.dhalo);
-    b.sx = g.dsx;
-    b.sxy = g.dsx * g.dsy;
-    b.on = it.tile >= 0;
-    return b;
-}
-
 __device__ __forceinline__ Box make_box(const Geom &g, const Item &it)
 {
     Box b;
