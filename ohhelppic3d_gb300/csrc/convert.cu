@@ -252,15 +252,29 @@ void launch_tiled(ohpic_ctx *c, int mode, int strict)
     // four per lane (FP32 push/deposit): the boxes end on a 16-byte boundary and are
     // followed by the per-thread prefetch stage (7 arrays x 256 threads x 16 bytes)
     if (!f64 && a.ppl == 4) smem = (a.sorted ? ((s3 * 4 * es + s3 * 8 + 15) & ~(size_t)15) : 0) + kQuadStageBytes + 128;
-    if (f64)
+    if (f64) {
         launch_tiled_f64(c, a, mode, strict, blocks, smem);
-    else
+        return;
+    }
+    // The push right after a sort reads the sort's records when it runs the
+    // default shape (four per lane, LANES deposit, tiles); anything else needs
+    // the word arrays first.
+    const bool from_rec = c->rec_pending && mode == MODE_PUSH && a.sorted && a.ppl == 4 &&
+                          a.deposit == OHPIC_DEPOSIT_LANES;
+    if (!from_rec) {
+        materialize_records(c);
         launch_tiled_f32(c, a, mode, blocks, smem);
+        return;
+    }
+    const RecIn rin{(const int4 *)c->pblock[1 - c->cur], c->ids[c->cur]};
+    launch_tiled_f32(c, a, mode, blocks, smem, &rin);
+    c->rec_pending = false;
 }
 
 void launch_f64_soa_from_stage(ohpic_ctx *c, const double *stage, int64_t n, int64_t dst, uint32_t id0, int aos,
                                int64_t stride_doubles)
 {
+    materialize_records(c);
     if (n <= 0) return;
     k_stage_to_f64<<<grid_for(n, 256), 256, 0, c->stream>>>(stage, n, aos, stride_doubles, c->p64[c->cur],
                                                              c->ids[c->cur], dst, id0);
@@ -270,6 +284,7 @@ void launch_f64_soa_from_stage(ohpic_ctx *c, const double *stage, int64_t n, int
 void launch_f64_to_f32(ohpic_ctx *c, const double *stage, int64_t n, int64_t dst, uint32_t id0, int aos,
                        int64_t stride_doubles)
 {
+    materialize_records(c);
     if (n <= 0) return;
     k_stage_to_f32<<<grid_for(n, 256), 256, 0, c->stream>>>(stage, n, aos, stride_doubles, c->p32[c->cur],
                                                              c->ids[c->cur], dst, id0, c->g.nx, c->g.ny,
@@ -279,6 +294,7 @@ void launch_f64_to_f32(ohpic_ctx *c, const double *stage, int64_t n, int64_t dst
 
 void launch_from_host_soa(ohpic_ctx *c, const Soa6 &s, int64_t n, int64_t dst, uint32_t id0)
 {
+    materialize_records(c);
     if (n <= 0) return;
     if (c->cfg.precision == OHPIC_FP64)
         k_soa_to_f64<<<grid_for(n, 256), 256, 0, c->stream>>>(s, n, c->p64[c->cur], c->ids[c->cur], dst, id0);
@@ -290,6 +306,7 @@ void launch_from_host_soa(ohpic_ctx *c, const Soa6 &s, int64_t n, int64_t dst, u
 
 void launch_to_host_soa(ohpic_ctx *c, const Soa6w &out, int64_t src, int64_t n)
 {
+    materialize_records(c);
     if (n <= 0) return;
     if (c->cfg.precision == OHPIC_FP64)
         k_f64_to_soa<<<grid_for(n, 256), 256, 0, c->stream>>>(c->p64[c->cur], src, n, out);
@@ -300,6 +317,7 @@ void launch_to_host_soa(ohpic_ctx *c, const Soa6w &out, int64_t src, int64_t n)
 
 void launch_to_f64_stage(ohpic_ctx *c, double *stage, int64_t src, int64_t n)
 {
+    materialize_records(c);
     if (n <= 0) return;
     if (c->cfg.precision == OHPIC_FP64)
         k_f64_to_stage<<<grid_for(n, 256), 256, 0, c->stream>>>(c->p64[c->cur], src, n, stage);
@@ -310,6 +328,7 @@ void launch_to_f64_stage(ohpic_ctx *c, double *stage, int64_t src, int64_t n)
 
 void launch_kinetic(ohpic_ctx *c)
 {
+    materialize_records(c);
     for (int s = 0; s < c->cfg.nspecies; ++s) {
         double *out = &c->diag->kin[s][0];
         cudaMemsetAsync(out, 0, 4 * sizeof(double), c->stream);

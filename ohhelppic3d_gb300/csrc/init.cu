@@ -192,6 +192,7 @@ int init_particles(ohpic_ctx *c, uint64_t initstate, uint64_t initseq, uint64_t 
     d.spi = spi;
     d.seg = c->seg;
     d.cap = c->cap;
+    materialize_records(c);
     d.p64 = c->p64[c->cur];
     d.p32 = c->p32[c->cur];
     d.ids = c->ids[c->cur];

@@ -242,6 +242,7 @@ int64_t snap_species_bytes(bool f64, int64_t n)
 // and their element sizes; returns the count.
 int snap_arrays(ohpic_ctx *c, int s, char *arr[7], int64_t es[7])
 {
+    materialize_records(c);
     const int64_t seg = c->seg[s];
     if (c->cfg.precision == OHPIC_FP64) {
         const PartF64 &q = c->p64[c->cur];
@@ -304,7 +305,7 @@ int ohpic_destroy(ohpic_ctx *c)
         dfree(c->pblock[b]);   // holds the particle arrays and the ids
     }
     dfree(c->rho); dfree(c->phi); dfree(c->epad); dfree(c->spec); dfree(c->green); dfree(c->wsum);
-    dfree(c->cell_count); dfree(c->cell_start); dfree(c->scan_tmp); dfree(c->tile_begin);
+    dfree(c->cell_count); dfree(c->cell_start); dfree(c->scan_tmp); dfree(c->key_table); dfree(c->tile_begin);
     dfree(c->stage); dfree(c->interp_buf); dfree(c->diag);
     if (c->diag_host) cudaFreeHost(c->diag_host);
     fields_teardown(c);
@@ -401,6 +402,7 @@ int ohpic_create(const ohpic_config *cfg, ohpic_ctx **out)
     if (rc == OHPIC_OK) rc = dalloc(c, &c->cell_count, g.ncell);
     if (rc == OHPIC_OK) rc = dalloc(c, &c->cell_start, g.ncell + 1);
     if (rc == OHPIC_OK) rc = dalloc(c, &c->scan_tmp, scan_tmp_elems(g.ncell));
+    if (rc == OHPIC_OK) rc = dalloc(c, &c->key_table, (int64_t)g.nx + g.ny + g.nz);
     if (rc == OHPIC_OK) rc = dalloc(c, &c->tile_begin, (int64_t)k.nspecies * (g.ntile + 1));
     if (rc == OHPIC_OK) {
         // Staging: chunks of up to 4M particles (6 doubles) and 3 full fields.
@@ -437,6 +439,7 @@ int ohpic_upload_particles_soa(ohpic_ctx *c, int s, const double *x, const doubl
     if (n > c->cap[s]) return fail(c, OHPIC_ERR_CAPACITY, "upload: " + std::to_string(n) + " > capacity");
     if (n > 0 && (!x || !y || !z || !vx || !vy || !vz)) return fail(c, OHPIC_ERR_INVALID, "upload: null array");
     cudaSetDevice(c->dev);
+    materialize_records(c);
     const int64_t chunk = std::max<int64_t>(1, c->stage_bytes / 48);
     double *stage = (double *)c->stage;
     const double *src[6] = {x, y, z, vx, vy, vz};
@@ -474,6 +477,7 @@ int ohpic_upload_particles(ohpic_ctx *c, int s, const void *pbuf, int64_t n, int
     if (n > c->cap[s]) return fail(c, OHPIC_ERR_CAPACITY, "upload: " + std::to_string(n) + " > capacity");
     if (n > 0 && !pbuf) return fail(c, OHPIC_ERR_INVALID, "upload: null buffer");
     cudaSetDevice(c->dev);
+    materialize_records(c);
     const int64_t chunk = std::max<int64_t>(1, c->stage_bytes / stride);
     for (int64_t a = 0; a < n; a += chunk) {
         const int64_t m = std::min(chunk, n - a);
@@ -501,6 +505,7 @@ int ohpic_init_particles(ohpic_ctx *c, uint64_t initstate, uint64_t initseq, uin
             return fail(c, OHPIC_ERR_INVALID, "init: ppc and vth must be finite and >= 0");
     }
     cudaSetDevice(c->dev);
+    materialize_records(c);
     const int rc = init_particles(c, initstate, initseq, advance, species, counts_out);
     if (rc != OHPIC_OK) return rc;
     return check_device(c);
@@ -515,6 +520,7 @@ int ohpic_download_particles_soa(ohpic_ctx *c, int s, double *x, double *y, doub
     if (capacity < n) return fail(c, OHPIC_ERR_CAPACITY, "download: host capacity too small");
     if (ids && !c->cfg.track_ids) return fail(c, OHPIC_ERR_INVALID, "download: ids requested but not tracked");
     cudaSetDevice(c->dev);
+    materialize_records(c);
     const int64_t chunk = std::max<int64_t>(1, c->stage_bytes / 48);
     double *stage = (double *)c->stage;
     double *dst[6] = {x, y, z, vx, vy, vz};
@@ -554,6 +560,7 @@ int ohpic_download_particles(ohpic_ctx *c, int s, void *pbuf, int64_t capacity, 
     if (n_out) *n_out = n;
     if (capacity < n) return fail(c, OHPIC_ERR_CAPACITY, "download: host capacity too small");
     cudaSetDevice(c->dev);
+    materialize_records(c);
     const int64_t chunk = std::max<int64_t>(1, c->stage_bytes / 48);
     double *stage = (double *)c->stage;
     for (int64_t a = 0; a < n; a += chunk) {
@@ -853,6 +860,7 @@ int ohpic_set_tuning(ohpic_ctx *c, const ohpic_tuning *t)
     if (!make_geom(c->cfg, t->tile, t->halo, g2))
         return fail(c, OHPIC_ERR_INVALID, "tuning: tile edges must divide the grid (<= 64) and the staged box fit");
     cudaSetDevice(c->dev);
+    materialize_records(c);
     const bool relayout = g2.tx != c->g.tx || g2.ty != c->g.ty || g2.tz != c->g.tz || g2.halo != c->g.halo;
     if (relayout) {
         OHPIC_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -902,6 +910,7 @@ int ohpic_snapshot_save(ohpic_ctx *c, void *host, int64_t bytes)
     ohpic_snapshot_size(c, &need);
     if (bytes < need) return fail(c, OHPIC_ERR_CAPACITY, "snapshot_save: buffer smaller than ohpic_snapshot_size");
     cudaSetDevice(c->dev);
+    materialize_records(c);
     const bool f64 = c->cfg.precision == OHPIC_FP64;
     SnapHeader h;
     memset(&h, 0, sizeof(h));
@@ -960,6 +969,7 @@ int ohpic_snapshot_load(ohpic_ctx *c, const void *host, int64_t bytes)
     }
     if (bytes < need) return fail(c, OHPIC_ERR_INVALID, "snapshot_load: truncated snapshot");
     cudaSetDevice(c->dev);
+    materialize_records(c);
     const char *p = (const char *)host + sizeof(h);
     for (int s = 0; s < h.nspecies; ++s) {
         const int64_t n = h.count[s];

@@ -123,6 +123,14 @@ struct TileArgs {
     int chunk;                         // particles per CTA when unsorted
 };
 
+// Sorted 32-byte particle records (sort.cu) read by the push that follows the
+// sort, and the ids array that push fills from them (null when ids are not
+// tracked).
+struct RecIn {
+    const int4 *rec;
+    uint32_t *ids;
+};
+
 // One run of the multi-run push (serve.cu): its tile arguments and current particles.
 constexpr int kMaxServeRuns = 512;
 struct RunDesc {
@@ -228,9 +236,14 @@ struct ohpic_ctx {
     uint32_t *cell_count;   // ncell
     uint32_t *cell_start;   // ncell + 1
     uint32_t *scan_tmp;
+    uint32_t *key_table;    // nx + ny + nz per-axis terms of the tile-major key
     int64_t *tile_begin;    // nspecies * (ntile + 1)
     bool sorted;
     int steps_since_sort;
+    // FP32 form: the last sort left every species as cell-sorted 32-byte records
+    // in pblock[1 - cur] and the word arrays are stale; the next push reads the
+    // records (and writes the arrays), anything else materialises them first.
+    bool rec_pending;
 
     // staging for uploads/downloads
     void *stage;
@@ -271,7 +284,12 @@ void species_consts(const ohpic_config &cfg, int s, double dt, SpeciesConst &k);
 // Kernel launchers: dispatch (convert.cu) and the two forms (push_f64.cu, push_f32.cu).
 void launch_tiled(ohpic_ctx *c, int mode, int strict);
 void launch_tiled_f64(ohpic_ctx *c, const TileArgs &a, int mode, int strict, int64_t blocks, size_t smem);
-void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks, size_t smem);
+void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks, size_t smem,
+                      const RecIn *rin = nullptr);
+// FP32 form: turns the sort's pending records back into the word arrays (no-op
+// when none are pending); every entry point that reads or writes particles
+// other than the push that consumes the records calls it first.
+void materialize_records(ohpic_ctx *c);
 cudaError_t launch_multi_f32(cudaStream_t st, int mode, int dep, int ppl, int weights, const MultiPush &m,
                              int grid, size_t smem);
 void ensure_emap(ohpic_ctx *c);

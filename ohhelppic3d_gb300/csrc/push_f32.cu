@@ -333,6 +333,40 @@ __device__ __forceinline__ void read_quad(const float4 *st, P32 r[4])
     }
 }
 
+// Record input: the push right after a cell sort reads the sort's 32-byte
+// records (cell, offsets | velocities, id) instead of the word arrays, and
+// writes the word arrays, so the sort needs no pass of its own to turn the
+// records back into arrays.  A quad's eight 16-byte record halves are
+// a0 b0 a1 b1 a2 b2 a3 b3 (a = cell and offsets, b = velocities and id); the
+// first seven go through the stage slots the seven arrays use, and b3 is
+// loaded into registers one quad ahead.
+__device__ __forceinline__ void prefetch_rec(float4 *st, const int4 *rec, int64_t g)
+{
+    const int n = blockDim.x, i = threadIdx.x;
+    const int4 *q = rec + 8 * g;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) cp_async16(st + k * n + i, q + k);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ void read_rec(const float4 *st, const int4 &b3, P32 r[4], uint4 &id)
+{
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    const int n = blockDim.x, i = threadIdx.x;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const float4 a = st[2 * j * n + i];
+        r[j].cell = __float_as_int(a.x);
+        r[j].ox = a.y; r[j].oy = a.z; r[j].oz = a.w;
+    }
+    const float4 b0 = st[n + i], b1 = st[3 * n + i], b2 = st[5 * n + i];
+    r[0].vx = b0.x; r[0].vy = b0.y; r[0].vz = b0.z;
+    r[1].vx = b1.x; r[1].vy = b1.y; r[1].vz = b1.z;
+    r[2].vx = b2.x; r[2].vy = b2.y; r[2].vz = b2.z;
+    r[3].vx = __int_as_float(b3.x); r[3].vy = __int_as_float(b3.y); r[3].vz = __int_as_float(b3.z);
+    id = make_uint4(__float_as_uint(b0.w), __float_as_uint(b1.w), __float_as_uint(b2.w), (unsigned)b3.w);
+}
+
 __device__ __forceinline__ void store_quad(const PartF32 &p, int64_t g, const P32 r[4])
 {
     *(int4 *)(p.cell + 4 * g) = make_int4(r[0].cell, r[1].cell, r[2].cell, r[3].cell);
@@ -536,11 +570,13 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
 // the lanes' last sums once per 128 particles.  The per-particle arithmetic is
 // advance(), as in the two-per-lane pass, and every sum is integer, so both
 // passes give the same bits.
-template <int MODE, int DEP, int W>
+template <int MODE, int DEP, int W, bool REC = false>
 __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap,
-                                           const Item &it, unsigned char *smem, uint64_t *ebar)
+                                           const Item &it, unsigned char *smem, uint64_t *ebar,
+                                           const RecIn &rin = RecIn{})
 {
     static_assert(MODE == MODE_PUSH || MODE == MODE_DEPOSIT, "four per lane: push or deposit");
+    static_assert(!REC || MODE == MODE_PUSH, "record input: push only");
     constexpr bool kGather = MODE != MODE_DEPOSIT;
     constexpr bool kMove = MODE == MODE_PUSH;
 
@@ -578,7 +614,15 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
     // Prefetch stage after the boxes (16-byte aligned); the launch reserves it.
     const size_t boxes = box.on ? ((kGather ? (size_t)s3 * sizeof(float4) : 0) + (size_t)s3 * 8 + 15) & ~(size_t)15 : 0;
     float4 *stage = (float4 *)(smem + boxes);
-    if (it.g0 + threadIdx.x < it.g1) prefetch_quad<kGather>(stage, p, it.g0 + threadIdx.x);
+    int4 b3 = make_int4(0, 0, 0, 0);   // REC: the current quad's last record half
+    if (it.g0 + threadIdx.x < it.g1) {
+        if (REC) {
+            prefetch_rec(stage, rin.rec, it.g0 + threadIdx.x);
+            b3 = __ldg(rin.rec + 8 * (it.g0 + threadIdx.x) + 7);
+        } else {
+            prefetch_quad<kGather>(stage, p, it.g0 + threadIdx.x);
+        }
+    }
 
     for (int64_t base = it.g0; base < it.g1; base += blockDim.x) {
         const int64_t gi = base + threadIdx.x;
@@ -588,8 +632,18 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
         for (int v = 0; v < 8; ++v) acc[v] = 0u;
         if (gi < it.g1) {
             P32 q[4];
-            read_quad<kGather>(stage, q);
-            if (gi + blockDim.x < it.g1) prefetch_quad<kGather>(stage, p, gi + blockDim.x);
+            uint4 qid;
+            int4 b3_next = make_int4(0, 0, 0, 0);
+            if (REC) {
+                read_rec(stage, b3, q, qid);
+                if (gi + blockDim.x < it.g1) {
+                    prefetch_rec(stage, rin.rec, gi + blockDim.x);
+                    b3_next = __ldg(rin.rec + 8 * (gi + blockDim.x) + 7);
+                }
+            } else {
+                read_quad<kGather>(stage, q);
+                if (gi + blockDim.x < it.g1) prefetch_quad<kGather>(stage, p, gi + blockDim.x);
+            }
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 if (4 * gi + j < end) {
@@ -609,6 +663,10 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
                 }
             }
             if (kMove) store_quad(p, gi, q);
+            if (REC) {
+                if (rin.ids) *(uint4 *)(rin.ids + 4 * gi) = qid;
+                b3 = b3_next;
+            }
         }
         warp_run_deposit<DEP>(acc_key, acc, slo, shi, box.sx, box.sxy);
     }
@@ -645,6 +703,19 @@ __global__ void __launch_bounds__(256, 2) tiled_f32(TileArgs a, PartF32 p, const
     __shared__ __align__(8) uint64_t ebar;
     // box start aligned to 128 bytes (the launch reserves the slack)
     run_item<MODE, DEP, PPL, W>(a, p, &emap, (int64_t)blockIdx.x, align128(smem_raw), &ebar);
+}
+
+// The push right after a sort, reading the sort's records (four per lane, LANES
+// deposit: the default launch shape); writes the word arrays p and the ids.
+template <int W>
+__global__ void __launch_bounds__(256, 2) tiled_f32_rec(TileArgs a, PartF32 p, RecIn rin,
+                                                        const __grid_constant__ CUtensorMap emap)
+{
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t ebar;
+    Item it;
+    if (get_item<4>(a, (int64_t)blockIdx.x, it))
+        tile_pass4<MODE_PUSH, OHPIC_DEPOSIT_LANES, W, true>(a, p, &emap, it, align128(smem_raw), &ebar, rin);
 }
 
 // Many contexts in one persistent launch.  Every CTA takes the next item from
@@ -744,11 +815,22 @@ static auto by_weights(int w, F f)
     return f(std::integral_constant<int, OHPIC_WEIGHTS_STANDARD>());
 }
 
-void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks, size_t smem)
+void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks, size_t smem, const RecIn *rin)
 {
     const PartF32 &pp = c->p32[c->cur];
     by_weights(a.weights, [&](auto w) {
         constexpr int W = decltype(w)::value;
+        if (rin) {
+            if (blocks <= 0) return 0;
+            auto kernel = tiled_f32_rec<W>;
+            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (smem > 96 * 1024)
+                cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     cudaSharedmemCarveoutMaxShared);
+            kernel<<<(unsigned)blocks, 256, smem, c->stream>>>(a, pp, *rin, c->emap);
+            ++c->launches;
+            return 0;
+        }
         if (mode == MODE_PUSH || mode == MODE_DEPOSIT) {
             by_lanes(a.ppl, [&](auto l) {
                 return by_deposit(a.deposit, [&](auto d) {

@@ -4,14 +4,16 @@
 // The sort makes the particles of one tile a contiguous range so the fused push
 // can stage that tile's fields in shared memory (push_f32.cu, push_f64.cu).
 //
-// Per species: histogram of cell keys (global atomics, aggregated per warp with
-// __match_any_sync), exclusive scan of the ncell counters (multi-level block
-// scan), tile start table, then a scatter of every particle as one whole
+// Per species: histogram of cell keys (global atomics, one per run of adjacent
+// lanes with equal keys), exclusive scan of the ncell counters (multi-level
+// block scan), tile start table, then a scatter of every particle as one whole
 // record (32 bytes in the FP32 form, 64 in the FP64 form) into the second
-// buffer's block, transposed back into the first buffer's arrays by a
-// sequential pass.  Lanes of a warp that share a key take consecutive slots in
-// lane order, so a warp's relative order is kept; order across warps follows the
-// atomic order.
+// buffer's block.  The FP64 form transposes the records back into the first
+// buffer's arrays at once; the FP32 form leaves them to the next push, which
+// reads the records directly (push_f32.cu), or to materialize_records.  In the
+// scatter, lanes of a warp that share a key (grouped with __match_any_sync) take
+// consecutive slots in lane order, so a warp's relative order is kept; order
+// across warps follows the atomic order.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -33,22 +35,48 @@ __device__ __forceinline__ uint32_t tile_key(const Geom &g, int ix, int iy, int 
     return tile * (uint32_t)g.tile_cells + (uint32_t)lx + (uint32_t)g.tx * ((uint32_t)ly + (uint32_t)g.ty * lz);
 }
 
-template <bool F32>
-__device__ __forceinline__ uint32_t particle_key(const Geom &g, const PartF64 &p64, const PartF32 &p32, int64_t i,
-                                                 DevDiag *d)
+// The tile-major key is a sum of one term per axis: with tile (TX, TY, TZ),
+//   key = [ (ix/TX) C + ix%TX ] + [ (iy/TY) NTX C + TX (iy%TY) ] + [ (iz/TZ) NTX NTY C + TX TY (iz%TZ) ]
+// (C = cells per tile, NTX/NTY tiles per row/plane), so the single-context sort
+// looks the three terms up in a table of nx + ny + nz entries built once per
+// sort (k_key_table) instead of dividing by the tile shape per particle.
+__global__ void k_key_table(Geom g, uint32_t *tab)
 {
-    int ix, iy, iz;
-    if (F32) {
-        const int32_t c = p32.cell[i];
-        ix = cell_x(c); iy = cell_y(c); iz = cell_z(c);
-    } else {
-        ix = (int)p64.x[i]; iy = (int)p64.y[i]; iz = (int)p64.z[i];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t C = (uint32_t)g.tile_cells;
+    if (i < g.nx) {
+        tab[i] = (uint32_t)(i / g.tx) * C + (uint32_t)(i % g.tx);
+    } else if (i < g.nx + g.ny) {
+        const int y = i - g.nx;
+        tab[i] = (uint32_t)(y / g.ty) * (uint32_t)g.ntx * C + (uint32_t)g.tx * (uint32_t)(y % g.ty);
+    } else if (i < g.nx + g.ny + g.nz) {
+        const int z = i - g.nx - g.ny;
+        tab[i] = (uint32_t)(z / g.tz) * (uint32_t)g.ntx * (uint32_t)g.nty * C +
+                 (uint32_t)(g.tx * g.ty) * (uint32_t)(z % g.tz);
     }
+}
+
+// Key of cell (ix, iy, iz) from the table when there is one, else by division;
+// a cell outside the grid flags OHPIC_ERR_BOUNDS and sorts as cell 0.
+__device__ __forceinline__ uint32_t cell_key(const Geom &g, const uint32_t *tab, int ix, int iy, int iz, DevDiag *d)
+{
     if ((unsigned)ix >= (unsigned)g.nx || (unsigned)iy >= (unsigned)g.ny || (unsigned)iz >= (unsigned)g.nz) {
         if (atomicCAS(&d->err_code, 0, OHPIC_ERR_BOUNDS) == 0) d->err_info = 10;
         ix = iy = iz = 0;
     }
+    if (tab) return __ldg(tab + ix) + __ldg(tab + g.nx + iy) + __ldg(tab + g.nx + g.ny + iz);
     return tile_key(g, ix, iy, iz);
+}
+
+template <bool F32>
+__device__ __forceinline__ uint32_t particle_key(const Geom &g, const uint32_t *tab, const PartF64 &p64,
+                                                 const PartF32 &p32, int64_t i, DevDiag *d)
+{
+    if (F32) {
+        const int32_t c = p32.cell[i];
+        return cell_key(g, tab, cell_x(c), cell_y(c), cell_z(c), d);
+    }
+    return cell_key(g, tab, (int)p64.x[i], (int)p64.y[i], (int)p64.z[i], d);
 }
 
 // Warp-aggregated atomicAdd of 1 per lane on count[key]; returns this lane's slot.
@@ -65,12 +93,28 @@ __device__ __forceinline__ uint32_t aggregated_inc(uint32_t *count, uint32_t key
     return base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
 }
 
+// Histogram add of 1 per active lane, one atomic per run of adjacent lanes with
+// equal keys.  Lanes hold consecutive particles and the particles are mostly in
+// cell order, so a warp holds a few runs; out-of-order keys just make more runs.
+__device__ __forceinline__ void run_count(uint32_t *count, uint32_t key, bool active)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t k = active ? key : 0xffffffffu - lane;   // inactive lanes end every run
+    const uint32_t prev = __shfl_up_sync(kFull, k, 1);
+    const bool head = lane == 0 || k != prev;
+    const unsigned heads = __ballot_sync(kFull, head);
+    const unsigned after = heads & ~((2u << lane) - 1u);   // run heads strictly after this lane
+    const unsigned end = after ? (unsigned)__ffs(after) - 1u : 32u;
+    if (active && head) atomicAdd(count + key, end - lane);
+}
+
 // The sort kernels are bound by memory latency (a cell load, then an atomic, then
 // the record), so each thread keeps several independent particles in flight:
 // four per iteration in the histogram, two in the scatter, whose record loads are
 // all issued before the atomics.
 template <bool F32>
-__global__ void k_hist(Geom g, PartF64 p64, PartF32 p32, int64_t seg, int64_t n, uint32_t *count, DevDiag *d)
+__global__ void k_hist(Geom g, const uint32_t *tab, PartF64 p64, PartF32 p32, int64_t seg, int64_t n,
+                       uint32_t *count, DevDiag *d)
 {
     constexpr int U = 4;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -81,10 +125,10 @@ __global__ void k_hist(Geom g, PartF64 p64, PartF32 p32, int64_t seg, int64_t n,
         for (int u = 0; u < U; ++u) {
             const int64_t i = base + u * stride + threadIdx.x;
             act[u] = i < n;
-            key[u] = act[u] ? particle_key<F32>(g, p64, p32, seg + i, d) : 0u;
+            key[u] = act[u] ? particle_key<F32>(g, tab, p64, p32, seg + i, d) : 0u;
         }
 #pragma unroll
-        for (int u = 0; u < U; ++u) aggregated_inc(count, key[u], act[u]);
+        for (int u = 0; u < U; ++u) run_count(count, key[u], act[u]);
     }
 }
 
@@ -113,19 +157,10 @@ __device__ __forceinline__ void rec_load(const PartF64 &s64, const PartF32 &s32,
 }
 
 template <bool F32>
-__device__ __forceinline__ uint32_t rec_key(const Geom &g, const Rec<F32> &r, DevDiag *d)
+__device__ __forceinline__ uint32_t rec_key(const Geom &g, const uint32_t *tab, const Rec<F32> &r, DevDiag *d)
 {
-    int ix, iy, iz;
-    if (F32) {
-        ix = cell_x(r.cell); iy = cell_y(r.cell); iz = cell_z(r.cell);
-    } else {
-        ix = (int)r.a[0]; iy = (int)r.a[1]; iz = (int)r.a[2];
-    }
-    if ((unsigned)ix >= (unsigned)g.nx || (unsigned)iy >= (unsigned)g.ny || (unsigned)iz >= (unsigned)g.nz) {
-        if (atomicCAS(&d->err_code, 0, OHPIC_ERR_BOUNDS) == 0) d->err_info = 10;
-        ix = iy = iz = 0;
-    }
-    return tile_key(g, ix, iy, iz);
+    if (F32) return cell_key(g, tab, cell_x(r.cell), cell_y(r.cell), cell_z(r.cell), d);
+    return cell_key(g, tab, (int)r.a[0], (int)r.a[1], (int)r.a[2], d);
 }
 
 // FP32 form: the scatter writes each particle as one 32-byte record (cell, three
@@ -141,8 +176,8 @@ __device__ __forceinline__ void rec32_store(int4 *rec, int64_t j, const Rec<true
     rec[2 * j + 1] = make_int4(__float_as_int(r.f[3]), __float_as_int(r.f[4]), __float_as_int(r.f[5]), (int)r.id);
 }
 
-__global__ void k_scatter_rec32(Geom g, PartF32 s32, const uint32_t *sid, int4 *rec, int64_t seg, int64_t n,
-                                const uint32_t *start, uint32_t *cursor, DevDiag *d)
+__global__ void k_scatter_rec32(Geom g, const uint32_t *tab, PartF32 s32, const uint32_t *sid, int4 *rec,
+                                int64_t seg, int64_t n, const uint32_t *start, uint32_t *cursor, DevDiag *d)
 {
     constexpr int U = 2;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -157,7 +192,7 @@ __global__ void k_scatter_rec32(Geom g, PartF32 s32, const uint32_t *sid, int4 *
             if (act[u]) rec_load<true>(PartF64{}, s32, sid, seg + i, r[u]);
         }
 #pragma unroll
-        for (int u = 0; u < U; ++u) key[u] = act[u] ? rec_key<true>(g, r[u], d) : 0u;
+        for (int u = 0; u < U; ++u) key[u] = act[u] ? rec_key<true>(g, tab, r[u], d) : 0u;
 #pragma unroll
         for (int u = 0; u < U; ++u) slot[u] = aggregated_inc(cursor, key[u], act[u]);
 #pragma unroll
@@ -190,8 +225,8 @@ __device__ __forceinline__ void rec64_store(double2 *rec, int64_t j, const Rec<f
     rec[4 * j + 3] = make_double2(__longlong_as_double((long long)r.id), 0.0);
 }
 
-__global__ void k_scatter_rec64(Geom g, PartF64 s64, const uint32_t *sid, double2 *rec, int64_t seg, int64_t n,
-                                const uint32_t *start, uint32_t *cursor, DevDiag *d)
+__global__ void k_scatter_rec64(Geom g, const uint32_t *tab, PartF64 s64, const uint32_t *sid, double2 *rec,
+                                int64_t seg, int64_t n, const uint32_t *start, uint32_t *cursor, DevDiag *d)
 {
     constexpr int U = 2;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -206,7 +241,7 @@ __global__ void k_scatter_rec64(Geom g, PartF64 s64, const uint32_t *sid, double
             if (act[u]) rec_load<false>(s64, PartF32{}, sid, seg + i, r[u]);
         }
 #pragma unroll
-        for (int u = 0; u < U; ++u) key[u] = act[u] ? rec_key<false>(g, r[u], d) : 0u;
+        for (int u = 0; u < U; ++u) key[u] = act[u] ? rec_key<false>(g, tab, r[u], d) : 0u;
 #pragma unroll
         for (int u = 0; u < U; ++u) slot[u] = aggregated_inc(cursor, key[u], act[u]);
 #pragma unroll
@@ -337,7 +372,7 @@ __global__ void k_hist_multi(MultiSort m)
         for (int64_t base = first; base < last; base += blockDim.x) {
             const int64_t i = base + threadIdx.x;
             const bool active = i < last;
-            const uint32_t key = active ? particle_key<true>(sg.g, PartF64{}, sg.p, sg.off + i, sg.diag) : 0u;
+            const uint32_t key = active ? particle_key<true>(sg.g, nullptr, PartF64{}, sg.p, sg.off + i, sg.diag) : 0u;
             aggregated_inc(m.count + sg.key_base, key, active);
         }
     }
@@ -361,7 +396,7 @@ __global__ void k_scatter_multi(MultiSort m)
             const bool active = i < last;
             Rec<true> r;
             if (active) rec_load<true>(PartF64{}, sg.p, sg.ids, sg.off + i, r);
-            const uint32_t key = active ? rec_key<true>(sg.g, r, sg.diag) : 0u;
+            const uint32_t key = active ? rec_key<true>(sg.g, nullptr, r, sg.diag) : 0u;
             const uint32_t slot = aggregated_inc(m.cursor + sg.key_base, key, active);
             if (active) rec32_store(sg.rec, sg.off + (int64_t)(m.start[sg.key_base + key] - base0) + slot, r);
         }
@@ -455,22 +490,39 @@ int launch_sort_finish_multi(cudaStream_t st, const MultiSort &m, int64_t chunks
     return launches;
 }
 
+void materialize_records(ohpic_ctx *c)
+{
+    if (!c->rec_pending) return;
+    const int4 *rec = (const int4 *)c->pblock[1 - c->cur];
+    for (int s = 0; s < c->cfg.nspecies; ++s) {
+        const int64_t n = c->count[s];
+        if (n <= 0) continue;
+        k_rec32_to_soa<<<grid_of(n), 256, 0, c->stream>>>(rec, c->seg[s], n, c->p32[c->cur], c->ids[c->cur]);
+        ++c->launches;
+    }
+    c->rec_pending = false;
+}
+
 int sort_particles(ohpic_ctx *c)
 {
     const Geom &g = c->g;
     const bool f32 = c->cfg.precision == OHPIC_FP32;
     const int src = c->cur, dst = 1 - c->cur;   // the records come back into the current buffer
+    materialize_records(c);
+    const int axes = g.nx + g.ny + g.nz;
+    k_key_table<<<(unsigned)((axes + 255) / 256), 256, 0, c->stream>>>(g, c->key_table);
+    ++c->launches;
     for (int s = 0; s < c->cfg.nspecies; ++s) {
         const int64_t n = c->count[s];
         int64_t *tb = c->tile_begin + (int64_t)s * (g.ntile + 1);
         cudaMemsetAsync(c->cell_count, 0, sizeof(uint32_t) * g.ncell, c->stream);
         if (n > 0) {
             if (f32)
-                k_hist<true><<<grid_of(n), 256, 0, c->stream>>>(g, c->p64[src], c->p32[src], c->seg[s], n,
-                                                                c->cell_count, c->diag);
+                k_hist<true><<<grid_of(n), 256, 0, c->stream>>>(g, c->key_table, c->p64[src], c->p32[src],
+                                                                c->seg[s], n, c->cell_count, c->diag);
             else
-                k_hist<false><<<grid_of(n), 256, 0, c->stream>>>(g, c->p64[src], c->p32[src], c->seg[s], n,
-                                                                 c->cell_count, c->diag);
+                k_hist<false><<<grid_of(n), 256, 0, c->stream>>>(g, c->key_table, c->p64[src], c->p32[src],
+                                                                 c->seg[s], n, c->cell_count, c->diag);
             ++c->launches;
         }
         scan_exclusive(c, c->cell_count, c->cell_start, g.ncell, c->scan_tmp);
@@ -479,19 +531,23 @@ int sort_particles(ohpic_ctx *c)
         ++c->launches;
         if (n > 0) {
             cudaMemsetAsync(c->cell_count, 0, sizeof(uint32_t) * g.ncell, c->stream);
-            // records in the other buffer's block, then back into this buffer
+            // records in the other buffer's block, then back into this buffer:
+            // FP32 by the next push (or materialize_records), FP64 here
             if (f32) {
                 int4 *rec = (int4 *)c->pblock[dst];
-                k_scatter_rec32<<<grid_of(n), 256, 0, c->stream>>>(g, c->p32[src], c->ids[src], rec, c->seg[s], n,
-                                                                   c->cell_start, c->cell_count, c->diag);
-                k_rec32_to_soa<<<grid_of(n), 256, 0, c->stream>>>(rec, c->seg[s], n, c->p32[src], c->ids[src]);
+                k_scatter_rec32<<<grid_of(n), 256, 0, c->stream>>>(g, c->key_table, c->p32[src], c->ids[src], rec,
+                                                                   c->seg[s], n, c->cell_start, c->cell_count,
+                                                                   c->diag);
+                ++c->launches;
+                c->rec_pending = true;
             } else {
                 double2 *rec = (double2 *)c->pblock[dst];
-                k_scatter_rec64<<<grid_of(n), 256, 0, c->stream>>>(g, c->p64[src], c->ids[src], rec, c->seg[s], n,
-                                                                   c->cell_start, c->cell_count, c->diag);
+                k_scatter_rec64<<<grid_of(n), 256, 0, c->stream>>>(g, c->key_table, c->p64[src], c->ids[src], rec,
+                                                                   c->seg[s], n, c->cell_start, c->cell_count,
+                                                                   c->diag);
                 k_rec64_to_soa<<<grid_of(n), 256, 0, c->stream>>>(rec, c->seg[s], n, c->p64[src], c->ids[src]);
+                c->launches += 2;
             }
-            c->launches += 2;
         }
     }
     c->sorted = true;

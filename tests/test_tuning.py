@@ -64,10 +64,10 @@ def test_fp32_state_identical_across_launch_shapes(ohpic):
 
 @pytest.mark.gpu
 def test_fp32_particles_outside_their_box_identical(ohpic):
-    """Without a re-sort, fast particles drift far outside their tile's staged box.
-    The four-per-lane pass queues those per warp and runs them 32 at a time; its
-    state must match the two-per-lane pass (every particle inline) and a run that
-    re-sorts before every step (no particle outside its box)."""
+    """Without a re-sort, fast particles drift far outside their tile's staged box
+    and take the global-memory gather and deposit.  The four-per-lane and
+    two-per-lane passes must then match a run that re-sorts before every step (no
+    particle outside its box)."""
     P = ohpic
     base = {"tile": (8, 8, 8), "halo": 1}
     ref_f, ref_p, ref_d = _run(P, dict(base, sort_every=1), steps=24, vth=4.0)
@@ -96,3 +96,48 @@ def test_autotuner_returns_a_valid_shape(ohpic):
     assert all(32 % t["tile"][d] == 0 for d in range(3))
     assert 0 <= t["halo"] <= 4 and t["split"] >= 1 and t["sort_every"] >= 1
     assert t["deposit"] in (P.DEPOSIT_RUNS, P.DEPOSIT_UNIFORM, P.DEPOSIT_MATCH, P.DEPOSIT_GROUPS, P.DEPOSIT_LANES)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tuning", [{}, {"halo": 1, "split": 2}, {"deposit": "RUNS"}])
+def test_push_from_sort_records_matches_arrays(ohpic, tuning):
+    """The FP32 sort leaves its 32-byte records pending and the next push (four
+    per lane, LANES deposit) reads them and writes the word arrays and ids
+    itself.  Turning the records back into arrays first (here: a download between
+    the sort and the push) must give the same bits: every particle (matched by
+    id; the slot order across warps follows the sort's atomics), rho and the
+    crossing counts.  Other shapes (RUNS) always push from the arrays."""
+    P = ohpic
+    if "deposit" in tuning:
+        tuning = dict(tuning, deposit=getattr(P, "DEPOSIT_" + tuning["deposit"]))
+    n = (32, 32, 16)
+    ppc = 8
+    qm = [-1.0, 0.01]
+    q = [1.0 / qm[0] / ppc, 0.01 / qm[1] / ppc]
+    sp = [P.species_init(ppc, 1.5), P.species_init(ppc, 0.15)]
+    cap = [2 * ppc * n[0] * n[1] * n[2] + 3] * 2          # odd capacity: segments not multiples of 4
+    cfg = P.make_config(n=n, dt=0.1, b0=(0.0, 0.0, 0.6), qm=qm, q=q, capacity=cap, precision=P.FP32, sort_every=0)
+    out = []
+    for materialise in (False, True):
+        with P.PicContext(cfg) as ctx:
+            if tuning:
+                ctx.set_tuning(**tuning)
+            ctx.init_particles(sp, seed=(42, 77))
+            ctx.sort()
+            ctx.step(0.1, 6)                               # drift, so the next sort moves particles
+            ctx.sort()
+            if materialise:
+                ctx.download(0)
+            ctx.step(0.1, 1)
+            ctx.sort()
+            ctx.step(0.1, 2)
+            parts = [ctx.download(s) for s in range(2)]
+            out.append((parts, ctx.field(P.RHO), ctx.diagnostics()))
+    (pa, ra, da), (pb, rb, db) = out
+    assert np.array_equal(ra, rb)
+    assert da["crossings"] == db["crossings"] and da["count"] == db["count"]
+    for s in range(2):
+        for k in ("x", "y", "z", "vx", "vy", "vz", "ids"):
+            assert np.array_equal(pa[s][k], pb[s][k]), (s, k)
+        # every id once: the record push carried the ids with their particles
+        assert np.array_equal(pa[s]["ids"], np.arange(len(pa[s]["ids"]), dtype=np.uint32))
