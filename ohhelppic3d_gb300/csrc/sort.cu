@@ -111,9 +111,11 @@ __device__ __forceinline__ void run_count(uint32_t *count, uint32_t key, bool ac
 // The sort kernels are bound by memory latency (a cell load, then an atomic, then
 // the record), so each thread keeps several independent particles in flight:
 // four per iteration in the histogram, two in the scatter, whose record loads are
-// all issued before the atomics.
+// all issued before the atomics.  Launch bounds keep enough warps resident: five
+// CTAs of 256 per SM for the histogram, four for the FP32 scatter (64 registers,
+// against 70 and three CTAs without the bound).
 template <bool F32>
-__global__ void k_hist(Geom g, const uint32_t *tab, PartF64 p64, PartF32 p32, int64_t seg, int64_t n,
+__global__ void __launch_bounds__(256, 5) k_hist(Geom g, const uint32_t *tab, PartF64 p64, PartF32 p32, int64_t seg, int64_t n,
                        uint32_t *count, DevDiag *d)
 {
     constexpr int U = 4;
@@ -176,7 +178,7 @@ __device__ __forceinline__ void rec32_store(int4 *rec, int64_t j, const Rec<true
     rec[2 * j + 1] = make_int4(__float_as_int(r.f[3]), __float_as_int(r.f[4]), __float_as_int(r.f[5]), (int)r.id);
 }
 
-__global__ void k_scatter_rec32(Geom g, const uint32_t *tab, PartF32 s32, const uint32_t *sid, int4 *rec,
+__global__ void __launch_bounds__(256, 4) k_scatter_rec32(Geom g, const uint32_t *tab, PartF32 s32, const uint32_t *sid, int4 *rec,
                                 int64_t seg, int64_t n, const uint32_t *start, uint32_t *cursor, DevDiag *d)
 {
     constexpr int U = 2;
