@@ -177,7 +177,11 @@ int ohpic_push(ohpic_ctx *ctx, double dt);
  * Scatters first if rho is stale. */
 int ohpic_step(ohpic_ctx *ctx, double dt, int nsteps);
 
-/* Periodic counting sort of every species by tile-major cell index. */
+/* Periodic counting sort of every species by tile-major cell index.  In the
+ * FP32 form the sort leaves each particle as a 32-byte record; the next
+ * ohpic_push/ohpic_step in the default launch shape reads the records and
+ * writes the particle arrays itself, and every other call that touches
+ * particles converts them first.  Callers see no difference but the timing. */
 int ohpic_sort(ohpic_ctx *ctx);
 
 /* Field exchange, nx*ny*nz doubles with x fastest.  Uploading rho or E
