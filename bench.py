@@ -219,6 +219,15 @@ def tune_form(P, wl, form, args) -> dict | None:
             "seconds": round(time.perf_counter() - t0, 2)}
 
 
+def record_pushes(form: str, applied: dict, steps: int, sort_every: int, lanes: int) -> int:
+    """Pushes among `steps` timed steps that read the sort's records: the first
+    push after each sort (timed_steps sorts at every multiple of sort_every), in
+    the FP32 form with four particles per lane and the LANES deposit."""
+    if form != "fp32" or not sort_every or applied["lane_particles"] != 4 or applied["deposit"] != lanes:
+        return 0
+    return sum(1 for i in range(steps) if i % sort_every == 0)
+
+
 def run_form(P, torch, dist, wl, form, args, sampler, peak):
     tuning = tune_form(P, wl, form, args)
     ctx = make_context(P, wl, form, args.weights, dist.local)
@@ -256,12 +265,7 @@ def run_form(P, torch, dist, wl, form, args, sampler, peak):
     value = n_total * args.steps / (ms_max / 1e3)
     avg_push_ms = st["push_ms"] / max(st["push_launches"], 1)
     push_bytes = n_local * PUSH_BYTES_PER_PARTICLE[form] + wl.ncell * PUSH_BYTES_PER_NODE[form]
-    # pushes that read the sort's records: the first push after each sort when
-    # the shape is four per lane with the LANES deposit
-    applied = ctx.get_tuning()
-    rec_pushes = 0
-    if form == "fp32" and applied["lane_particles"] == 4 and applied["deposit"] == P.DEPOSIT_LANES and wl.sort_every:
-        rec_pushes = sum(1 for i in range(args.steps) if i % wl.sort_every == 0)
+    rec_pushes = record_pushes(form, ctx.get_tuning(), args.steps, wl.sort_every, P.DEPOSIT_LANES)
     push_bytes += rec_pushes * n_local * REC_PUSH_EXTRA_BYTES / max(st["push_launches"], 1)
     achieved = push_bytes / (avg_push_ms / 1e3) / 1e9
     step_bytes = n_local * PUSH_BYTES_PER_PARTICLE[form] + wl.ncell * STEP_BYTES_PER_NODE[form]

@@ -73,3 +73,19 @@ def test_single_rank_dist_is_a_no_op():
     assert not d.pg and d.max(2.5) == 2.5 and d.sum(3.0) == 3.0
     d.barrier()
     d.close()
+
+
+def test_record_push_count():
+    """The push roofline counts 8 more bytes per particle for each push that reads
+    the sort's records: one per sort in the timed steps, default shape only."""
+    sys.path.insert(0, ROOT)
+    import bench
+    lanes = 4
+    shape = {"lane_particles": 4, "deposit": lanes}
+    assert bench.record_pushes("fp32", shape, 20, 20, lanes) == 1
+    assert bench.record_pushes("fp32", shape, 41, 20, lanes) == 3
+    assert bench.record_pushes("fp32", shape, 5, 1, lanes) == 5
+    assert bench.record_pushes("fp32", shape, 20, 0, lanes) == 0
+    assert bench.record_pushes("fp64", shape, 20, 20, lanes) == 0
+    assert bench.record_pushes("fp32", dict(shape, lane_particles=2), 20, 20, lanes) == 0
+    assert bench.record_pushes("fp32", dict(shape, deposit=0), 20, 20, lanes) == 0
