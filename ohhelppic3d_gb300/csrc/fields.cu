@@ -112,6 +112,109 @@ __global__ void k_stencil(Geom g, const T *phi, NodeT *epad)
         stencil_node<T, NodeT>(g, phi, epad, t);
 }
 
+// ---- FP32 form: rho from the fixed-point weight sums ----
+//
+// rho = sum_s q_s * W_s * 2^-24 (W_s the species' integer weight sum at the
+// node), rounded once to FP32.  Each charge is an integer mantissa times a power
+// of two (from its bit pattern), so the sum is formed exactly in 128-bit integer
+// arithmetic and rounded to nearest, ties to even: no FP64 arithmetic per node.
+// Bounds: |m_s| < 2^53, W_s < 2^58 (every count is far below 2^34), the exponent
+// spread at most kRhoMaxShift, at most 8 species: the sum stays below 2^126.
+// Charges further apart in exponent (or subnormal), and sums outside the normal
+// FP32 range, take the FP64 expression instead.
+constexpr int kRhoMaxShift = 12;
+
+struct RhoScale {
+    long long m[OHPIC_MAX_SPECIES];
+    int shift[OHPIC_MAX_SPECIES];
+    int K;
+    bool ok;
+};
+
+__device__ __forceinline__ RhoScale rho_scale(const double *q, int nsp)
+{
+    RhoScale r;
+    r.ok = true;
+    r.K = 0x7fffffff;
+    int k[OHPIC_MAX_SPECIES];
+    for (int s = 0; s < nsp; ++s) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(q[s]);
+        const int e = (int)((b >> 52) & 0x7ffu);
+        const long long mant = (long long)(b & ((1ull << 52) - 1));
+        r.m[s] = 0;
+        k[s] = 0;
+        if (e == 0) {
+            if (mant != 0) r.ok = false;   // subnormal charge
+            continue;
+        }
+        if (e == 0x7ff) {
+            r.ok = false;
+            continue;
+        }
+        const long long m = mant | (1ll << 52);
+        r.m[s] = (b >> 63) ? -m : m;
+        k[s] = e - 1075 - 24;              // q_s * 2^-24 = m * 2^k
+        r.K = min(r.K, k[s]);
+    }
+    for (int s = 0; s < nsp; ++s) {
+        r.shift[s] = r.m[s] != 0 ? k[s] - r.K : 0;
+        if (r.shift[s] > kRhoMaxShift) r.ok = false;
+    }
+    if (r.K == 0x7fffffff) r.K = 0;        // every charge zero: the sum is 0
+    return r;
+}
+
+// acc * 2^K rounded to FP32, nearest with ties to even; false outside the
+// normal range.
+__device__ __forceinline__ bool i128_to_float_rne(__int128 acc, int K, float &out)
+{
+    if (acc == 0) {
+        out = 0.f;
+        return true;
+    }
+    const bool neg = acc < 0;
+    const unsigned __int128 a = neg ? (unsigned __int128)(-acc) : (unsigned __int128)acc;
+    const unsigned long long hi = (unsigned long long)(a >> 64), lo = (unsigned long long)a;
+    int msb = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);
+    unsigned int mant;
+    if (msb <= 23) {
+        mant = (unsigned int)(lo << (23 - msb));
+    } else {
+        const int sh = msb - 23;
+        const unsigned __int128 one = 1;
+        const unsigned __int128 rem = a & ((one << sh) - 1);
+        const unsigned __int128 half = one << (sh - 1);
+        mant = (unsigned int)(a >> sh);
+        if (rem > half || (rem == half && (mant & 1u))) {
+            ++mant;
+            if (mant == (1u << 24)) {
+                mant >>= 1;
+                ++msb;
+            }
+        }
+    }
+    const int be = msb + K + 127;
+    if (be < 1 || be > 254) return false;
+    out = __uint_as_float((neg ? 0x80000000u : 0u) | ((unsigned)be << 23) | (mant & 0x7fffffu));
+    return true;
+}
+
+// rho at one node: w[s * stride] is species s's weight sum.
+__device__ __forceinline__ float node_rho(const unsigned long long *w, int64_t stride, int nsp, const double *q,
+                                          const RhoScale &r)
+{
+    if (r.ok) {
+        __int128 acc = 0;
+        for (int s = 0; s < nsp; ++s)
+            if (r.m[s] != 0) acc += ((__int128)r.m[s] * (__int128)(long long)w[s * stride]) << r.shift[s];
+        float v;
+        if (i128_to_float_rne(acc, r.K, v)) return v;
+    }
+    double acc = 0.0;
+    for (int s = 0; s < nsp; ++s) acc += q[s] * (double)w[s * stride];
+    return (float)(acc * kWeightUnit);
+}
+
 // ---- pooled fields: many runs of one grid size, slot = blockIdx.y; on[slot] == 0 skips ----
 
 // rho of every active slot from its fixed-point weight sums (nsp species per slot,
@@ -124,13 +227,12 @@ __global__ void k_pool_rho(unsigned long long *w, int64_t ncell, int nsp, const 
     w += (int64_t)slot * nsp * ncell;
     rho += (int64_t)slot * ncell;
     q += (int64_t)slot * nsp;
+    __shared__ RhoScale r;
+    if (threadIdx.x == 0) r = rho_scale(q, nsp);
+    __syncthreads();
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ncell; t += (int64_t)gridDim.x * blockDim.x) {
-        double acc = 0.0;
-        for (int s = 0; s < nsp; ++s) {
-            acc += q[s] * (double)w[s * ncell + t];
-            w[s * ncell + t] = 0ull;
-        }
-        rho[t] = (float)(acc * kWeightUnit);
+        rho[t] = node_rho(w + t, ncell, nsp, q, r);
+        for (int s = 0; s < nsp; ++s) w[s * ncell + t] = 0ull;
     }
 }
 
@@ -228,7 +330,7 @@ __global__ void k_field_sums(Geom g, const T *rho, const NodeT *epad, double *ch
 }
 
 // FP32 form: rho = sum_s q_s * W_s * 2^-24 from the fixed-point weight sums,
-// evaluated in FP64 and rounded once to FP32.
+// summed exactly and rounded once to FP32 (node_rho).
 struct SpeciesCharges {
     double q[OHPIC_MAX_SPECIES];
     int nspecies;
@@ -236,11 +338,11 @@ struct SpeciesCharges {
 
 __global__ void k_wsum_to_rho(const unsigned long long *w, int64_t ncell, SpeciesCharges sc, float *rho)
 {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ncell; t += (int64_t)gridDim.x * blockDim.x) {
-        double acc = 0.0;
-        for (int s = 0; s < sc.nspecies; ++s) acc += sc.q[s] * (double)w[s * ncell + t];
-        rho[t] = (float)(acc * kWeightUnit);
-    }
+    __shared__ RhoScale r;
+    if (threadIdx.x == 0) r = rho_scale(sc.q, sc.nspecies);
+    __syncthreads();
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ncell; t += (int64_t)gridDim.x * blockDim.x)
+        rho[t] = node_rho(w + t, ncell, sc.nspecies, sc.q, r);
 }
 
 int blocks_for(int64_t n)
