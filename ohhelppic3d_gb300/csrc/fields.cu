@@ -205,8 +205,16 @@ __device__ __forceinline__ float node_rho(const unsigned long long *w, int64_t s
 {
     if (r.ok) {
         __int128 acc = 0;
-        for (int s = 0; s < nsp; ++s)
-            if (r.m[s] != 0) acc += ((__int128)r.m[s] * (__int128)(long long)w[s * stride]) << r.shift[s];
+        for (int s = 0; s < nsp; ++s) {
+            const long long m = r.m[s];
+            if (m == 0) continue;
+            // |m| * W as one 64 x 64 -> 128-bit product, then the species' shift
+            const unsigned long long W = w[s * stride];
+            const unsigned long long am = (unsigned long long)(m < 0 ? -m : m);
+            unsigned __int128 p = ((unsigned __int128)__umul64hi(am, W) << 64) | (unsigned __int128)(am * W);
+            p <<= r.shift[s];
+            acc = m < 0 ? acc - (__int128)p : acc + (__int128)p;
+        }
         float v;
         if (i128_to_float_rne(acc, r.K, v)) return v;
     }
