@@ -146,8 +146,6 @@ int check_device(ohpic_ctx *c)
 
 bool species_ok(const ohpic_ctx *c, int s) { return c && s >= 0 && s < c->cfg.nspecies; }
 
-int ensure_fields(ohpic_ctx *c);
-
 // Clears the deposit target: rho (FP64 form) or the per-species fixed-point
 // weight sums (FP32 form, turned into rho by the next solve or download).
 void zero_deposit(ohpic_ctx *c)
