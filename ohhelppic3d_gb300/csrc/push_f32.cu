@@ -27,6 +27,12 @@
 // particles per lane.  The box is flushed once per CTA into per-species 64-bit
 // global sums.  All of it is integer addition, so the deposit does not depend on
 // the order in which atomics land.
+//
+// After a cell sort.  The sort (sort.cu) leaves every particle as a 32-byte
+// record in the second buffer; the next push (tiled_f32_rec) reads those
+// records in place of the seven arrays and writes the arrays and the ids, so
+// the sort has no transpose pass of its own.  The arithmetic is the same
+// advance(), so both pushes give the same bits.
 #include <type_traits>
 
 #include "tile_common.cuh"
