@@ -79,6 +79,12 @@ void species_consts(const ohpic_config &cfg, int s, double dt, SpeciesConst &k)
     const double tt = k.t[0] * k.t[0] + k.t[1] * k.t[1] + k.t[2] * k.t[2];
     for (int d = 0; d < 3; ++d) k.s[d] = 2.0 * k.t[d] / (1.0 + tt);
     k.mass = k.q / k.qm;
+    k.hq32 = (float)(k.qm * k.dt2);
+    k.dt32 = (float)dt;
+    for (int d = 0; d < 3; ++d) {
+        k.t32[d] = (float)k.t[d];
+        k.s32[d] = (float)k.s[d];
+    }
 }
 
 // The device address of a host array the GPU can reach directly (pinned with

@@ -72,6 +72,10 @@ struct SpeciesConst {
     double t[3];           // qm*B*dt2 (:42)
     double s[3];           // 2t/(1+|t|^2) (:43)
     double mass;           // q/qm
+    // The FP32 push's constants, rounded once on the host from the values
+    // above: qm*dt2, dt, t, s.  Read as floats, the kernel never converts (a
+    // conversion from double runs on GB300's narrow FP64 pipe).
+    float hq32, dt32, t32[3], s32[3];
 };
 
 // One FP64 E node (Ex, Ey, Ez, pad), 32-byte aligned.

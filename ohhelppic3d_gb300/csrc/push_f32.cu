@@ -522,10 +522,10 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
     const int sp = it.sp;
     const SpeciesConst &c = a.sc[sp];
     Push32 k;
-    k.hq = (float)(c.qm * c.dt2);
-    k.dt = (float)c.dt;
-    k.t0 = (float)c.t[0]; k.t1 = (float)c.t[1]; k.t2 = (float)c.t[2];
-    k.s0 = (float)c.s[0]; k.s1 = (float)c.s[1]; k.s2 = (float)c.s[2];
+    k.hq = c.hq32;
+    k.dt = c.dt32;
+    k.t0 = c.t32[0]; k.t1 = c.t32[1]; k.t2 = c.t32[2];
+    k.s0 = c.s32[0]; k.s1 = c.s32[1]; k.s2 = c.s32[2];
     const int64_t end = a.seg[sp] + a.count[sp];
     Tally t;
 
@@ -611,10 +611,10 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
     const int sp = it.sp;
     const SpeciesConst &c = a.sc[sp];
     Push32 k;
-    k.hq = (float)(c.qm * c.dt2);
-    k.dt = (float)c.dt;
-    k.t0 = (float)c.t[0]; k.t1 = (float)c.t[1]; k.t2 = (float)c.t[2];
-    k.s0 = (float)c.s[0]; k.s1 = (float)c.s[1]; k.s2 = (float)c.s[2];
+    k.hq = c.hq32;
+    k.dt = c.dt32;
+    k.t0 = c.t32[0]; k.t1 = c.t32[1]; k.t2 = c.t32[2];
+    k.s0 = c.s32[0]; k.s1 = c.s32[1]; k.s2 = c.s32[2];
     const int64_t end = a.seg[sp] + a.count[sp];
     Tally t;
     // Prefetch stage after the boxes (16-byte aligned); the launch reserves it.
