@@ -1,21 +1,31 @@
 """Benchmark of the particle hot path: particle-steps/s on one GB300 (or N replicas).
 
 Default workload: the 256^3 configuration (2 species x 32 ppc = 1,073,741,824
-particles), run in the FP32 precision form (headline `value`) and the plain
-FP64 form (`fp64_form`).  A step is one mainstep: spectral field solve, then
-the fused gather + Boris + periodic wrap + deposit over every particle; the
-cell sort runs every 20 steps counted from the first timed step (so a timed
-region of K <= 20 steps always contains one sort), and the warm-up runs whole
-sort cycles, so the timed sort follows a full cycle of particle drift.
+particles).  The headline `value` is the FP32 precision form with standard CIC
+weights, the convention in which it meets the error bar; `fp64_form` is the
+plain FP64 form on the same workload.  A step is one mainstep: spectral field
+solve, then the fused gather + Boris + periodic wrap + deposit over every
+particle, with the cell sort before every step whose index is a multiple of 20.
+
+Each (form, convention) is one run from the injector: whole sort cycles of
+warm-up, the K timed steps, then on to step 100.  Fields are captured after
+steps 1, 10 and 100, outside the timed window, and the FP32 run's captures are
+compared with the FP64 run's from the same seeds (`accuracy`).  The FP32 form in
+the reference's own swapped-weight convention is run the same way beside it,
+with its own error.  Also in the line: the 32^3 configuration's errors against
+the oracle itself (`c3_vs_oracle`), the clustered two-stream workload (`c4`),
+both forms end to end through the C ABI (`e2e`), the oracle on the host cores
+(`cpu_baseline`) and the serving ensemble (`serving`).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload c2|c1|c4] [--forms fp32,fp64] [--no-e2e] [--no-cpu-baseline]
+                  [--workload c2|c1|c4] [--forms fp32,fp64] [--weights 1|0] [--no-e2e] ...
 
 For N > 1 (launched with torch.distributed.run) every rank advances its own
 replica of the workload (different random streams); there is no collective on
 the data path ("replicas only"), only a barrier and a max-reduction of the
 timings.  `--impl reference` times the reference's CPU path (the C restatement
-in oracle/, since the Fortran reference cannot be built) on the host cores.
+in oracle/, since the Fortran reference cannot be built) on the host cores, on
+a slab of the workload with the same plasma.
 """
 from __future__ import annotations
 
@@ -44,10 +54,17 @@ PUSH_BYTES_PER_NODE = {"fp32": 12 + 4, "fp64": 24 + 8}
 STEP_BYTES_PER_NODE = {"fp32": 72, "fp64": 144}
 # DRAM traffic of one push launch over its algorithmic bytes, from one ncu capture of
 # the push (dram__bytes_read.sum + dram__bytes_write.sum) at 128x128x64 with the same
-# tuned tile, halo and particle density (profiles/push_f32_128x128x64.md,
-# profiles/push_f64_128x128x64.md): 3.799 / 3.775 GB and 6.622 / 6.476 GB.  Both
-# terms scale with the grid at fixed density, so the ratio carries to 256^3.
+# tuned tile, halo and particle density: 3.799 / 3.775 GB (FP32) and 6.622 / 6.476 GB
+# (FP64).  Both terms scale with the grid at fixed density, so the ratio carries to
+# 256^3.
 PUSH_TRAFFIC_RATIO = {"fp32": 3.799238 / 3.774873600, "fp64": 6.621735 / 6.476005376}
+PUSH_TRAFFIC_SOURCE = {
+    "fp32": "ncu DRAM bytes of one push launch at 128x128x64 (same tile, halo and density), scaled by particles",
+    "fp64": "ncu DRAM bytes of one push launch at 128x128x64 (same tile, halo and density), scaled by particles",
+}
+# The precision form's accuracy target: E-field relative L2 error against the FP64
+# run after 100 steps.
+E_ERROR_BAR = 1e-5
 
 
 def _peaks():
@@ -175,6 +192,9 @@ class Dist:
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+CHECKPOINTS = (1, 10, 100)
+
+
 def make_context(P, wl, form: str, weights: int, device: int):
     caps = [c + 1024 for c in wl.counts()]
     cfg = P.make_config(n=wl.n, dt=wl.dt, b0=wl.b0, qm=[s.qm for s in wl.species], q=[s.q for s in wl.species],
@@ -188,20 +208,12 @@ def species_inits(P, wl):
             for s in wl.species]
 
 
-def timed_steps(ctx, wl, k: int, on_step=None):
-    for i in range(k):
-        if wl.sort_every and i % wl.sort_every == 0:
-            ctx.sort()
-        ctx.step(wl.dt, 1)
-        if on_step is not None:
-            on_step()
-
-
-def tune_form(P, wl, form, args) -> dict | None:
+def tune_form(P, wl, form, args, weights) -> dict | None:
     """Launch shape for this workload from the autotuner, measured on a proxy grid
     of at most 256 x 128 x 64 cells with the same particles per cell and physics,
     each candidate ranked by its mean push over one sort cycle (the sort cadence
-    stays the workload's)."""
+    stays the workload's).  The weight convention does not change the kernels'
+    work, so one tuning serves both conventions."""
     if args.tuning:
         return dict(json.loads(args.tuning), tuned_on="given on the command line")
     if args.no_tune:
@@ -210,7 +222,7 @@ def tune_form(P, wl, form, args) -> dict | None:
     t0 = time.perf_counter()
     t = autotune.tune(n=wl.n, dt=wl.dt, b0=wl.b0, qm=[s.qm for s in wl.species], q=[s.q for s in wl.species],
                       capacity_per_cell=[s.ppc * 1.02 + 1 for s in wl.species], species=species_inits(P, wl),
-                      precision=P.FP32 if form == "fp32" else P.FP64, weights=args.weights,
+                      precision=P.FP32 if form == "fp32" else P.FP64, weights=weights,
                       steps=max(4, wl.sort_every - 1) if form == "fp32" else 4,
                       max_cadence=40, proxy_limit=(256, 128, 64))
     keep = ("tile", "halo", "split", "deposit", "lane_particles")
@@ -221,28 +233,87 @@ def tune_form(P, wl, form, args) -> dict | None:
 
 def record_pushes(form: str, applied: dict, steps: int, sort_every: int, lanes: int) -> int:
     """Pushes among `steps` timed steps that read the sort's records: the first
-    push after each sort (timed_steps sorts at every multiple of sort_every), in
+    push after each sort (the course sorts at every multiple of sort_every), in
     the FP32 form with four particles per lane and the LANES deposit."""
     if form != "fp32" or not sort_every or applied["lane_particles"] != 4 or applied["deposit"] != lanes:
         return 0
     return sum(1 for i in range(steps) if i % sort_every == 0)
 
 
-def run_form(P, torch, dist, wl, form, args, sampler, peak):
-    tuning = tune_form(P, wl, form, args)
-    ctx = make_context(P, wl, form, args.weights, dist.local)
+def capture(P, ctx) -> dict:
+    """The state at the current step: rho, phi and E (FP64 host copies, solved
+    from the particles' current charge) and the diagnostics."""
+    ctx.solve()
+    f = {name: ctx.field(w) for name, w in (("rho", P.RHO), ("phi", P.PHI), ("ex", P.EX), ("ey", P.EY),
+                                             ("ez", P.EZ))}
+    return {"fields": f, "diag": ctx.diagnostics()}
+
+
+def _rel_l2(a, b) -> float:
+    import numpy as np
+    return float(np.linalg.norm(a - b) / max(float(np.linalg.norm(b)), 1e-300))
+
+
+def compare(got: dict, ref: dict) -> dict:
+    """Relative L2 errors of rho, phi, each E component and E as a whole, and the
+    relative difference of the field energy, of `got` against `ref`."""
+    import numpy as np
+    g, r = got["fields"], ref["fields"]
+    out = {k: _rel_l2(g[k], r[k]) for k in ("rho", "phi", "ex", "ey", "ez")}
+    num = sum(float(np.linalg.norm(g[k] - r[k])) ** 2 for k in ("ex", "ey", "ez"))
+    den = sum(float(np.linalg.norm(r[k])) ** 2 for k in ("ex", "ey", "ez"))
+    out["e"] = (num / max(den, 1e-300)) ** 0.5
+    wr = ref["diag"]["field_energy"]
+    out["field_energy_rel_diff"] = (got["diag"]["field_energy"] - wr) / wr if wr else None
+    return out
+
+
+def energy_drift(caps: dict) -> dict:
+    """Total (kinetic + field) energy at each checkpoint relative to step 0."""
+    e0 = caps[0]["diag"]["kinetic_energy"] + caps[0]["diag"]["field_energy"]
+    return {str(k): (v["diag"]["kinetic_energy"] + v["diag"]["field_energy"] - e0) / e0
+            for k, v in sorted(caps.items()) if k}
+
+
+def run_course(P, torch, dist, wl, form, weights, args, sampler, peak, tuning, checkpoints=()):
+    """One run of the workload from the injector: whole sort cycles of warm-up (at
+    least --warmup steps), the K timed steps, then on to the last checkpoint.  The
+    cell sort runs before every step whose index is a multiple of sort_every, so
+    the timed window's first sort meets particles that drifted for a full cycle,
+    as every sort of a long run does.  `checkpoints` are steps after which the
+    fields are captured (outside the timed window; step 0 is always captured
+    when any is asked for).  Returns the context, the per-species counts, the
+    timing result and the captures."""
+    ctx = make_context(P, wl, form, weights, dist.local)
     if tuning:
         from ohhelppic3d_gb300 import autotune
         autotune.apply(ctx, tuning, keep_sort_every=True)
     counts = ctx.init_particles(species_inits(P, wl), seed=(42, 52 + dist.rank))
     n_local = sum(counts)
-    # warm-up in whole sort cycles (at least --warmup steps), so that the timed
-    # region's first sort meets particles that drifted for a full cycle, as every
-    # sort of a long run does
-    warm = -(-args.warmup // wl.sort_every) * wl.sort_every if wl.sort_every else args.warmup
-    if not wl.sort_every:
-        ctx.sort()
-    timed_steps(ctx, wl, warm)
+    se = wl.sort_every
+    warm = -(-args.warmup // se) * se if se else args.warmup
+    t_end = warm + args.steps
+    inside = [c for c in checkpoints if warm < c <= t_end]
+    if inside:
+        raise ValueError(f"checkpoints {inside} fall inside the timed window ({warm}, {t_end}]")
+    caps = {0: capture(P, ctx)} if checkpoints else {}
+    step = 0
+
+    def advance(target, on_step=None):
+        nonlocal step
+        while step < target:
+            if se and step % se == 0:
+                ctx.sort()
+            elif not se and step == 0:
+                ctx.sort()
+            ctx.step(wl.dt, 1)
+            step += 1
+            if on_step is not None:
+                on_step()
+            if step in checkpoints:
+                caps[step] = capture(P, ctx)
+
+    advance(warm)
     ctx.synchronize()
     ctx.set_push_timing(True)
     launches0 = ctx.stats()["launches"]
@@ -252,7 +323,7 @@ def run_form(P, torch, dist, wl, form, args, sampler, peak):
     torch.cuda.synchronize()
     sampler.start()
     e0.record(stream)
-    timed_steps(ctx, wl, args.steps)
+    advance(t_end)
     e1.record(stream)
     e1.synchronize()
     torch.cuda.synchronize()
@@ -260,12 +331,15 @@ def run_form(P, torch, dist, wl, form, args, sampler, peak):
     dist.barrier()
     ms = e0.elapsed_time(e1)
     st = ctx.stats()
+    ctx.set_push_timing(False)
+    launches = st["launches"] - launches0
+    advance(max([t_end] + list(checkpoints)))
     ms_max = dist.max(ms)
     n_total = dist.sum(float(n_local))
     value = n_total * args.steps / (ms_max / 1e3)
     avg_push_ms = st["push_ms"] / max(st["push_launches"], 1)
     push_bytes = n_local * PUSH_BYTES_PER_PARTICLE[form] + wl.ncell * PUSH_BYTES_PER_NODE[form]
-    rec_pushes = record_pushes(form, ctx.get_tuning(), args.steps, wl.sort_every, P.DEPOSIT_LANES)
+    rec_pushes = record_pushes(form, ctx.get_tuning(), args.steps, se, P.DEPOSIT_LANES)
     push_bytes += rec_pushes * n_local * REC_PUSH_EXTRA_BYTES / max(st["push_launches"], 1)
     achieved = push_bytes / (avg_push_ms / 1e3) / 1e9
     step_bytes = n_local * PUSH_BYTES_PER_PARTICLE[form] + wl.ncell * STEP_BYTES_PER_NODE[form]
@@ -274,37 +348,47 @@ def run_form(P, torch, dist, wl, form, args, sampler, peak):
         "roofline": {"bound": "hbm", "kernel": f"tiled_{'f32' if form == 'fp32' else 'f64'}<MODE_PUSH> (fused push)",
                      "achieved": achieved, "peak": peak[0], "unit": "GB/s", "frac": achieved / peak[0],
                      "traffic": PUSH_TRAFFIC_RATIO[form] * push_bytes, "bytes_per_launch": push_bytes,
-                     "avg_launch_ms": avg_push_ms, "record_pushes": rec_pushes, "peak_source": peak[1],
-                     "traffic_source": "ncu DRAM bytes of one push launch at 128x128x64, scaled by particles "
-                                       "(the record push measured the same ratio within 0.1%)"},
+                     "avg_launch_ms": avg_push_ms, "record_pushes": rec_pushes,
+                     "peak_source": f"{peak[1]} (MEASURED_PEAKS.json hbm_gbs: copy bandwidth)",
+                     "traffic_source": PUSH_TRAFFIC_SOURCE[form]},
         "step_hbm_frac": step_bytes / (ms_max / args.steps / 1e3) / 1e9 / peak[0],
         "push_share": st["push_ms"] / ms if ms > 0 else None,
-        "gpu_launches": st["launches"] - launches0,
+        "gpu_launches": launches,
         "tuning": dict(tuning or {}, applied=ctx.get_tuning()),
-        "sort_every": wl.sort_every,
+        "sort_every": se,
         "warmup_steps_run": warm,
+        "timed_steps": [warm, t_end],
+        "weights": _wname(weights),
     }
-    return ctx, counts, out
+    return ctx, counts, out, caps
 
 
-def run_e2e(P, torch, dist, wl, form, args, ctx, counts):
+def pinned_host_arrays(torch, wl) -> list:
+    """Pinned FP64 host arrays (x, y, z, vx, vy, vz) per species, with room for the
+    injector's counts; allocated once and shared by the e2e runs of both forms."""
+    return [{k: torch.empty(c + 1024, dtype=torch.float64, pin_memory=True).numpy()
+             for k in ("x", "y", "z", "vx", "vy", "vz")} for c in wl.counts()]
+
+
+def run_e2e(P, torch, dist, wl, args, ctx, counts, host):
     """The same K steps through the C ABI with host buffers: upload every particle
     from pinned host memory, K steps each followed by a diagnostics read (the
     step's result: charge and energies), and a download of every particle."""
     import numpy as np
-    host = []
     for s, n in enumerate(counts):
-        arrs = {k: torch.empty(max(n, 1), dtype=torch.float64, pin_memory=True).numpy()
-                for k in ("x", "y", "z", "vx", "vy", "vz")}
-        ctx.download_into(s, arrs)
-        host.append(arrs)
+        ctx.download_into(s, host[s])
     ctx.set_energy_tracking(True)
     ctx.synchronize()
+    se = wl.sort_every
     dist.barrier()
     t0 = time.perf_counter()
     for s, n in enumerate(counts):
         ctx.upload_n(s, host[s], n)
-    timed_steps(ctx, wl, args.steps, on_step=ctx.diagnostics)
+    for i in range(args.steps):
+        if (se and i % se == 0) or (not se and i == 0):
+            ctx.sort()
+        ctx.step(wl.dt, 1)
+        ctx.diagnostics()
     for s in range(len(counts)):
         ctx.download_into(s, host[s])
     ctx.synchronize()
@@ -319,13 +403,68 @@ def run_e2e(P, torch, dist, wl, form, args, ctx, counts):
             "d2h_bytes_per_step": (moved + args.steps * 160) / args.steps,
             "seconds": sec, "finite": finite,
             "how": ("job through the C ABI: ohpic_upload_particles_soa from pinned FP64 host arrays, "
-                    "K x (ohpic_step + ohpic_diagnostics), ohpic_download_particles_soa")}
+                    "K x (ohpic_sort every sort_every steps + ohpic_step + ohpic_diagnostics), "
+                    "ohpic_download_particles_soa")}
+
+
+def c3_vs_oracle(P, weights_list, threads: int) -> dict:
+    """The precision form (and the plain form) of the 32^3 configuration against
+    the oracle itself: the same initial particles uploaded to the GPU and to the
+    oracle, 100 steps with a sort every 20, fields compared after 1, 10 and 100
+    steps.  The FP32 form meets the 1e-5 bar only with the continuous (standard)
+    CIC weights; the reference's swapped weights are discontinuous at cell faces."""
+    import oracle as O
+    from ohhelppic3d_gb300.workloads import c1
+    wl = c1()
+    out = {"workload": wl.description, "threads": threads}
+    for w in weights_list:
+        setup = O.Setup(n=wl.n, dt=wl.dt, b0=wl.b0, weights=w,
+                        species=[O.SpeciesInit(ppc=s.ppc, vth=s.vth, qm=s.qm, q=s.q) for s in wl.species])
+        o = O.Oracle(setup, threads=threads)
+        o.init_particles()
+        parts = [o.get_particles(s) for s in range(len(wl.species))]
+        ref = {}
+        done = 0
+        for step in CHECKPOINTS:
+            o.step(step - done)
+            done = step
+            o.deposit()
+            o.solve()
+            ref[step] = {"fields": {k: o.get_field(getattr(O, k.upper())) for k in ("rho", "phi", "ex", "ey", "ez")},
+                         "diag": o.diagnostics()}
+        o.close()
+        for form in ("fp32", "fp64"):
+            caps = [len(p["x"]) + 64 for p in parts]
+            cfg = P.make_config(n=wl.n, dt=wl.dt, b0=wl.b0, qm=[s.qm for s in wl.species],
+                                q=[s.q for s in wl.species], capacity=caps,
+                                precision=P.FP32 if form == "fp32" else P.FP64, weights=w, sort_every=20)
+            with P.PicContext(cfg) as ctx:
+                for s, p in enumerate(parts):
+                    ctx.upload(s, p)
+                errs, done = {}, 0
+                for step in CHECKPOINTS:
+                    ctx.step(wl.dt, step - done)
+                    done = step
+                    errs[str(step)] = compare(capture(P, ctx), ref[step])
+            out[f"{form}_{'standard' if w else 'reference'}_weights"] = errs
+    return out
+
+
+def accuracy_block(caps32: dict, caps64: dict, weights: int) -> dict:
+    steps = {str(k): compare(caps32[k], caps64[k]) for k in CHECKPOINTS}
+    e100 = steps[str(CHECKPOINTS[-1])]["e"]
+    return {"against": ("the plain FP64 form on the GPU from the same injector seeds and weight convention "
+                        "(oracle-checked on the 32^3 configuration: cell indices and crossings exact, "
+                        "fields within 2e-12 after 100 steps)"),
+            "weights": _wname(weights), "steps": steps, "e_rel_l2_after_100": e100,
+            "bar": E_ERROR_BAR, "meets_bar": e100 <= E_ERROR_BAR,
+            "energy_drift": {"fp32": energy_drift(caps32), "fp64": energy_drift(caps64)}}
 
 
 # ---------------------------------------------------------------------------
 # Serving: the ensemble of small runs through the continuous-batching server
 # ---------------------------------------------------------------------------
-def sequential_runs(P, reqs, sort_every: int) -> dict:
+def sequential_runs(P, reqs, sort_every: int, weights: int) -> dict:
     """One run at a time on the single-context API: create, draw, step, read the
     diagnostics, destroy.  Times with and without the per-run set-up."""
     import torch
@@ -336,7 +475,7 @@ def sequential_runs(P, reqs, sort_every: int) -> dict:
         t0 = time.perf_counter()
         caps = [c + 64 for c in _req_counts(r)]
         cfg = P.make_config(n=r.n, dt=r.dt, b0=r.b0, qm=r.qm, q=r.q, capacity=caps, precision=P.FP32,
-                            sort_every=sort_every)
+                            weights=weights, sort_every=sort_every)
         with P.PicContext(cfg) as ctx:
             # the server's launch shape: halo 1, tile edges up to 16 in x and 8 in y, z
             tile = tuple(max(t for t in (1, 2, 4, 8, 16) if t <= want and n % t == 0)
@@ -374,23 +513,23 @@ def run_serving(P, args) -> dict:
     from ohhelppic3d_gb300 import serve as S
     n_runs, scale = args.serve_runs, args.serve_step_scale
     sat_reqs = S.ensemble_stream(n_runs, rate=None, step_scale=scale)
-    with S.Server(sort_every=args.serve_sort_every) as srv:
+    with S.Server(sort_every=args.serve_sort_every, weights=args.weights) as srv:
         sat = S.run_stream(srv, sat_reqs)
         sat_stats = srv.stats()
     mean_work = sat["particle_steps"] / n_runs
     rate = 0.8 * sat["throughput"] / mean_work
     reqs = S.ensemble_stream(n_runs, rate=rate, step_scale=scale)
-    with S.Server(sort_every=args.serve_sort_every) as srv:
+    with S.Server(sort_every=args.serve_sort_every, weights=args.weights) as srv:
         poi = S.run_stream(srv, reqs)
         poi_stats = srv.stats()
     k = min(args.serve_sequential, n_runs)
-    seq = sequential_runs(P, sat_reqs[:k], args.serve_sort_every)
+    seq = sequential_runs(P, sat_reqs[:k], args.serve_sort_every, args.weights)
     keep = ("ticks", "sort_ticks", "graph_captures", "graph_launches", "launches", "bytes_peak", "pools")
     return {
         "workload": (f"{n_runs} periodic FP32 runs: grids {{16,24,32,48,64}}^3, ppc per species {{8,16,32,64}}, "
                      f"wce/wpe~U[0,1], vth_e~U[0.5,2], vth_i=vth_e/10, mass ratio 100, dt=0.1, "
                      f"steps~U{{200..2000}} x {scale}; parameter stream pcg32 (42, 1000), run i seeded (42, 52+i)"),
-        "runs": n_runs, "step_scale": scale, "particle_steps": sat["particle_steps"],
+        "runs": n_runs, "step_scale": scale, "weights": _wname(args.weights), "particle_steps": sat["particle_steps"],
         "saturated": {"throughput": sat["throughput"], "span_s": sat["span_s"], "p50_s": sat["p50_s"],
                       "p99_s": sat["p99_s"], "stats": {k2: sat_stats[k2] for k2 in keep}},
         "poisson_80": {"rate_runs_per_s": rate, "throughput": poi["throughput"], "span_s": poi["span_s"],
@@ -406,34 +545,45 @@ def run_serving(P, args) -> dict:
 # ---------------------------------------------------------------------------
 # CPU path (oracle): the reference's algorithm on the host cores
 # ---------------------------------------------------------------------------
-def cpu_sample_step(wl, fraction: float, threads: int, weights: int, steps: int = 1):
-    """Times `steps` mainsteps of the oracle on `fraction` of the workload's
-    particles (full grid), returning the extrapolated full-workload seconds per step."""
+CPU_SAMPLE_PARTICLES = 6.8e7
+
+
+def cpu_sample_workload(wl):
+    """A bounded sample of the workload for the CPU path: the same plasma (density,
+    species, physics) on a slab of the box, the z extent cut to the largest power
+    of two that keeps about 6.8e7 particles.  Every per-particle and per-node cost
+    is the workload's own, measured directly rather than scaled."""
+    import copy
+    if wl.nparticles <= CPU_SAMPLE_PARTICLES:
+        return wl
+    nz = wl.n[2]
+    while nz > 1 and wl.nparticles * nz / wl.n[2] > CPU_SAMPLE_PARTICLES:
+        nz //= 2
+    s = copy.deepcopy(wl)
+    s.n = (wl.n[0], wl.n[1], nz)
+    s.description = f"{wl.n[0]}x{wl.n[1]}x{nz} slab of: {wl.description}"
+    return s
+
+
+def oracle_course(wl, threads: int, weights: int, steps: int, warmup: int):
+    """`warmup` untimed then `steps` timed mainsteps (deposit + FFT solve + push) of
+    the oracle on the workload; returns the per-step seconds and the particle count."""
     import oracle as O
-    species = [O.SpeciesInit(ppc=s.ppc * fraction, vth=s.vth, qm=s.qm, q=s.q, drift=s.drift, lo=s.lo, hi=s.hi)
+    species = [O.SpeciesInit(ppc=s.ppc, vth=s.vth, qm=s.qm, q=s.q, drift=s.drift, lo=s.lo, hi=s.hi)
                for s in wl.species]
     setup = O.Setup(n=wl.n, dt=wl.dt, b0=wl.b0, species=species, weights=weights)
     o = O.Oracle(setup, threads=threads)
     o.init_particles()
-    n_sample = sum(o.count(i) for i in range(len(species)))
-    per_step = []
+    n = sum(o.count(i) for i in range(len(species)))
+    for _ in range(warmup):
+        o.step(1)
+    times = []
     for _ in range(steps):
         t0 = time.perf_counter()
-        o.deposit()
-        t1 = time.perf_counter()
-        o.solve()
-        t2 = time.perf_counter()
-        o.push()
-        t3 = time.perf_counter()
-        t_particles = (t1 - t0) + (t3 - t2)
-        per_step.append(t_particles * wl.nparticles / n_sample + (t2 - t1))
+        o.step(1)
+        times.append(time.perf_counter() - t0)
     o.close()
-    return per_step, n_sample
-
-
-def cpu_sample_fraction(wl) -> float:
-    # about 6.7e7 sampled particles at 256^3; the whole workload when it is small
-    return min(1.0, 6.7e7 / max(wl.nparticles, 1))
+    return times, n
 
 
 def run_reference(args, wl):
@@ -441,21 +591,22 @@ def run_reference(args, wl):
     if dist.rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    frac = cpu_sample_fraction(wl)
-    warm, _ = cpu_sample_step(wl, frac, threads, args.weights, steps=max(args.warmup, 0) and 1)
-    times, n_sample = cpu_sample_step(wl, frac, threads, args.weights, steps=args.steps)
+    sample = cpu_sample_workload(wl)
+    times, n_sample = oracle_course(sample, threads, args.weights, args.steps, min(args.warmup, 2))
     sec = sum(times)
-    value = wl.nparticles * args.steps / sec
-    sample = (f"{args.steps} mainsteps (deposit + FFT solve + push) of the oracle on {n_sample} of the "
-              f"{wl.nparticles} particles (uniform over the full {wl.n[0]}x{wl.n[1]}x{wl.n[2]} grid); "
-              f"particle time scaled to the full count, field solve counted once per step")
+    value = n_sample * args.steps / sec
+    what = (f"{args.steps} timed mainsteps (deposit + FFT solve + push, after {min(args.warmup, 2)} untimed) of "
+            f"the oracle with {threads} OpenMP threads on {n_sample} particles: {sample.description}; "
+            f"throughput measured on that sample, not scaled")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
         "data": "synthetic: pcg32 seeds (42, 52), the reference injector's draw order",
-        "config": {"workload": wl.description, "form": "reference CPU path (FP64)", "weights": _wname(args.weights)},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "config": {"workload": wl.description, "sample": sample.description,
+                   "form": "reference CPU path (FP64; the oracle restatement, the Fortran reference cannot be built)",
+                   "weights": _wname(args.weights)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": what},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -466,6 +617,11 @@ def _wname(w: int) -> str:
     return "reference (swapped CIC, linear_scatter.f90:41-52)" if w == 0 else "standard CIC"
 
 
+def _short(res: dict, keys=("value", "ms_per_step", "particles", "roofline", "step_hbm_frac", "push_share",
+                             "gpu_launches", "tuning", "sort_every", "weights")) -> dict:
+    return {k: res[k] for k in keys if k in res}
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -474,7 +630,13 @@ def main(argv=None) -> int:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c4"])
     ap.add_argument("--forms", default="fp32,fp64")
-    ap.add_argument("--weights", type=int, default=0)
+    ap.add_argument("--weights", type=int, default=1,
+                    help="CIC convention of the headline: 1 standard (default), 0 the reference's swapped weights")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the error checkpoints against the FP64 form")
+    ap.add_argument("--no-other-weights", action="store_true",
+                    help="skip the FP32 run in the other CIC convention")
+    ap.add_argument("--no-c3", action="store_true", help="skip the 32^3 errors against the oracle")
+    ap.add_argument("--no-c4", action="store_true", help="skip the clustered two-stream block")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n", default=None, help="grid override nx,ny,nz (same physics and ppc; for profiling)")
@@ -484,7 +646,7 @@ def main(argv=None) -> int:
                     help='fixed launch shape instead of the autotuner, e.g. \'{"tile": [16, 8, 8], "halo": 1}\'')
     ap.add_argument("--serve-only", action="store_true", help="only the ensemble serving measurement")
     ap.add_argument("--serve-runs", type=int, default=512)
-    ap.add_argument("--serve-step-scale", type=float, default=0.1)
+    ap.add_argument("--serve-step-scale", type=float, default=1.0)
     ap.add_argument("--serve-sort-every", type=int, default=8)
     ap.add_argument("--serve-sequential", type=int, default=32, help="runs timed one at a time")
     args = ap.parse_args(argv)
@@ -508,6 +670,7 @@ def main(argv=None) -> int:
     peak = _peaks()
     forms = [f.strip() for f in args.forms.split(",") if f.strip()]
     sampler = ClockSampler(dist.local)
+    solo = dist.rank == 0 and dist.world == 1
     if args.serve_only:
         sampler.start()
         serving = run_serving(P, args)
@@ -516,25 +679,65 @@ def main(argv=None) -> int:
             print(json.dumps({"metric": METRIC, "serving": serving, "clocks": sampler.summary()}), flush=True)
         dist.close()
         return 0
-    results = {}
-    e2e = None
-    for i, form in enumerate(forms):
-        ctx, counts, res = run_form(P, torch, dist, wl, form, args, sampler, peak)
-        if i == 0 and not args.no_e2e:
-            e2e = run_e2e(P, torch, dist, wl, form, args, ctx, counts)
+
+    accuracy = not args.no_accuracy and "fp32" in forms and "fp64" in forms
+    checkpoints = CHECKPOINTS if accuracy else ()
+    other_w = 1 - args.weights
+    tunings = {f: tune_form(P, wl, f, args, args.weights) for f in forms}
+    results, caps, e2e = {}, {}, {}
+    host = None if args.no_e2e else pinned_host_arrays(torch, wl)
+    # the plain FP64 form first, so its captures are at hand when the FP32 run ends
+    for form in sorted(forms, key=lambda f: f != "fp64"):
+        ctx, counts, res, cp = run_course(P, torch, dist, wl, form, args.weights, args, sampler, peak,
+                                          tunings[form], checkpoints)
+        if not args.no_e2e:
+            e2e[form] = run_e2e(P, torch, dist, wl, args, ctx, counts, host)
         ctx.close()
         torch.cuda.empty_cache()
-        results[form] = res
+        results[form], caps[form] = res, cp
+    acc = accuracy_block(caps["fp32"], caps["fp64"], args.weights) if accuracy else None
+    caps.clear()
+    host = None
+
+    other = None
+    if "fp32" in forms and not args.no_other_weights:
+        cp64 = cp32 = {}
+        if accuracy:
+            ctx, _, _, cp64 = run_course(P, torch, dist, wl, "fp64", other_w, args, sampler, peak,
+                                         tunings.get("fp64"), checkpoints)
+            ctx.close()
+            torch.cuda.empty_cache()
+        ctx, _, res, cp32 = run_course(P, torch, dist, wl, "fp32", other_w, args, sampler, peak,
+                                       tunings["fp32"], checkpoints)
+        ctx.close()
+        torch.cuda.empty_cache()
+        other = _short(res)
+        if accuracy:
+            other["accuracy"] = accuracy_block(cp32, cp64, other_w)
+        del cp64, cp32
+
+    c3 = None
+    if solo and not args.no_c3:
+        c3 = c3_vs_oracle(P, (args.weights, other_w), os.cpu_count() or 1)
+
+    c4 = None
+    if args.workload == "c2" and not args.no_c4 and not args.n:
+        from ohhelppic3d_gb300.workloads import c4 as c4_workload
+        w4 = c4_workload()
+        t4 = tune_form(P, w4, "fp32", args, args.weights)
+        ctx, _, res, _ = run_course(P, torch, dist, w4, "fp32", args.weights, args, sampler, peak, t4)
+        ctx.close()
+        torch.cuda.empty_cache()
+        c4 = dict(_short(res), workload=w4.description)
 
     cpu = None
-    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+    if solo and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        frac = cpu_sample_fraction(wl)
-        times, n_sample = cpu_sample_step(wl, frac, threads, args.weights, steps=2)
-        sec = times[-1]
-        cpu = {"value": wl.nparticles / sec, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": (f"1 timed mainstep (after 1 untimed) of the oracle on {n_sample} of {wl.nparticles} "
-                          f"particles over the full grid; particle time scaled to the full count, field solve once")}
+        sample = cpu_sample_workload(wl)
+        times, n_sample = oracle_course(sample, threads, args.weights, 1, 1)
+        cpu = {"value": n_sample / times[-1], "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": (f"1 timed mainstep (after 1 untimed) of the oracle with {threads} OpenMP threads on "
+                          f"{n_sample} particles: {sample.description}; measured on that sample, not scaled")}
 
     serving = None
     if not args.no_serve and dist.world == 1:
@@ -550,26 +753,30 @@ def main(argv=None) -> int:
         "config": {"workload": wl.description, "form": {"fp32": "FP32 precision form (int32 cell + FP32 offset)",
                                                         "fp64": "plain FP64 form"}[head],
                    "weights": _wname(args.weights), "particles": r["particles"], "sort_every": r["sort_every"],
-                   "warmup_steps_run": r["warmup_steps_run"],
+                   "warmup_steps_run": r["warmup_steps_run"], "timed_steps": r["timed_steps"],
                    "l2": (f"inputs larger than L2: {r['particles'] * (28 if head == 'fp32' else 48) / 1e9:.1f} GB "
                           f"of particle state per GPU against a 129 MB L2"),
                    "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU"},
         "roofline": r["roofline"],
+        "accuracy": acc if head == "fp32" else None,
         "tuning": r["tuning"],
         "step_hbm_frac": r["step_hbm_frac"],
         "gpu_launches": r["gpu_launches"],
         "clocks": sampler.summary(),
-        "e2e": e2e,
+        "e2e": e2e.get(head),
         "cpu_baseline": cpu,
     }
     for form, res in results.items():
         if form != head:
-            line[f"{form}_form"] = {"value": res["value"], "ms_per_step": res["ms_per_step"],
-                                   "dtype": "f64" if form == "fp64" else "f32", "roofline": res["roofline"],
-                                   "step_hbm_frac": res["step_hbm_frac"], "gpu_launches": res["gpu_launches"],
-                                   "tuning": res["tuning"]}
+            line[f"{form}_form"] = dict(_short(res), dtype="f64" if form == "fp64" else "f32", e2e=e2e.get(form))
     if "fp64" in results and head == "fp32":
         line["fp32_over_fp64"] = results["fp32"]["value"] / results["fp64"]["value"]
+    if other is not None:
+        line[f"fp32_{'reference' if other_w == 0 else 'standard'}_weights"] = other
+    if c3 is not None:
+        line["c3_vs_oracle"] = c3
+    if c4 is not None:
+        line["c4"] = c4
     if serving is not None:
         line["serving"] = serving
     if dist.rank == 0:

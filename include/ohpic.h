@@ -14,8 +14,8 @@
  * particle across a language boundary cannot feed a GPU, so this ABI offers the
  * same operations batched over every particle of the run, with the particles
  * and fields resident in device memory between calls.  The Fortran side binds
- * these functions with ISO_C_BINDING (the interface block is given in
- * INTEGRATION.md).
+ * these functions with ISO_C_BINDING interfaces whose derived types mirror the
+ * structs below field by field.
  *
  * Conventions
  *   - Every function returns an int status: OHPIC_OK (0) or an OHPIC_ERR_* code.
@@ -124,7 +124,10 @@ int ohpic_destroy(ohpic_ctx *ctx);
  * six doubles are x, y, z, vx, vy, vz, i.e. the leading members of the
  * reference's oh_particle (src/ohhelp/ohparticles.f90:17, used by
  * particle_injector_with_distribution.f90:196-201).  Upload replaces the
- * species' particles; n may be 0. */
+ * species' particles; n may be 0.  The FP32 form refuses positions it cannot
+ * wrap into the grid (OHPIC_ERR_BOUNDS) and positions or velocities that are
+ * not finite in FP32 (OHPIC_ERR_NONFINITE); a refused upload leaves the
+ * species empty. */
 int ohpic_upload_particles(ohpic_ctx *ctx, int species, const void *pbuf, int64_t n,
                            int64_t stride_bytes);
 int ohpic_upload_particles_soa(ohpic_ctx *ctx, int species, const double *x, const double *y,
@@ -220,6 +223,15 @@ int ohpic_diagnostics(ohpic_ctx *ctx, ohpic_diag *out);
  * the particles. */
 int ohpic_set_energy_tracking(ohpic_ctx *ctx, int enable);
 
+/* Fault injection for tests of the bounded device wait (no reference
+ * counterpart).  A push stages each tile's E box into shared memory with one
+ * TMA copy and waits for it at most `polls` polls of its mbarrier (default
+ * 2^22).  With polls = 0 every wait gives up at once: the kernel gathers from
+ * global memory instead, so the particles come out the same, waits the copy out
+ * before the CTA finishes, and the next call that synchronises (download,
+ * diagnostics, ohpic_synchronize) returns OHPIC_ERR_TIMEOUT. */
+int ohpic_set_tma_wait_limit(ohpic_ctx *ctx, uint32_t polls);
+
 /* The per-particle bindings of the reference cannot be served from device
  * memory; the batched calls above replace them.  These return
  * OHPIC_ERR_UNSUPPORTED so a caller that still loops per particle fails loudly. */
@@ -278,8 +290,9 @@ int ohpic_memory(ohpic_ctx *ctx, int64_t *device_bytes);
  * particle, exact per-particle sum), so the result is independent of atomic order.
  * The only scratch is a static device array of 2^21 nodes (16 MiB), held by every
  * GPU that loads the library until the process exits; larger grids return
- * OHPIC_ERR_CAPACITY.  The first call on a device looks up that array's device
- * address (cudaGetSymbolAddress) with the device current.  Every call on a device
+ * OHPIC_ERR_CAPACITY.  Every call looks up that array's device address
+ * (cudaGetSymbolAddress, which allocates nothing) in the current device's context,
+ * so a device reset between calls is harmless.  Every call on a device
  * shares the array and leaves it cleared, so calls that overlap on the GPU (two
  * streams, or two host threads) race and corrupt each other's results. */
 int ohpic_scatter_noalloc(const double *x, const double *y, const double *z, int64_t n, double charge,

@@ -122,6 +122,7 @@ SIGNATURES = {
                                                C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "ohpic_diagnostics": (C.c_int, [_P, C.POINTER(Diag)]),
     "ohpic_set_energy_tracking": (C.c_int, [_P, C.c_int]),
+    "ohpic_set_tma_wait_limit": (C.c_int, [_P, C.c_uint32]),
     "ohpic_move_one": (C.c_int, [_P, _DP, C.c_double, _DP, C.c_double]),
     "ohpic_scatter_one": (C.c_int, [_P, _DP, C.c_double, C.c_int]),
     "ohpic_last_error": (C.c_int, [_P, C.c_char_p, C.c_size_t]),
@@ -371,6 +372,10 @@ class PicContext:
 
     def set_energy_tracking(self, on: bool):
         self._check(lib().ohpic_set_energy_tracking(self.ptr, 1 if on else 0))
+
+    def set_tma_wait_limit(self, polls: int):
+        """Polls allowed for each tile's staged E box (0: every wait gives up at once)."""
+        self._check(lib().ohpic_set_tma_wait_limit(self.ptr, int(polls)))
 
     # -- instrumentation ------------------------------------------------------
     def set_push_timing(self, on: bool):

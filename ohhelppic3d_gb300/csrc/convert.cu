@@ -49,6 +49,12 @@ __global__ void k_stage_to_f64(const double *stage, int64_t n, int aos, int64_t 
 // FP32; a value that rounds up to 1 moves to offset 0 of the next cell.
 __device__ __forceinline__ void split_pos(double x, int n, int &i, float &o, DevDiag *d)
 {
+    if (!isfinite(x)) {   // floor(NaN) converts to cell 0 with a NaN offset: refuse it
+        flag_error(d, OHPIC_ERR_NONFINITE, 12);
+        i = 0;
+        o = 0.f;
+        return;
+    }
     int c = (int)floor(x);
     float f = (float)(x - (double)c);
     if (f >= 1.f) { f = 0.f; ++c; }
@@ -60,6 +66,13 @@ __device__ __forceinline__ void split_pos(double x, int n, int &i, float &o, Dev
     }
     i = c;
     o = f;
+}
+
+// The FP32 push trusts its particles (no per-particle checks), so an upload
+// refuses velocities that are not finite in FP32.
+__device__ __forceinline__ void check_velocity(double vx, double vy, double vz, DevDiag *d)
+{
+    if (!(isfinite((float)vx) && isfinite((float)vy) && isfinite((float)vz))) flag_error(d, OHPIC_ERR_NONFINITE, 13);
 }
 
 __global__ void k_stage_to_f32(const double *stage, int64_t n, int aos, int64_t stride, PartF32 p, uint32_t *ids,
@@ -77,6 +90,7 @@ __global__ void k_stage_to_f32(const double *stage, int64_t n, int aos, int64_t 
         p.cell[o] = pack_cell(ix, iy, iz);
         p.ox[o] = ox; p.oy[o] = oy; p.oz[o] = oz;
         p.vx[o] = (float)r[3]; p.vy[o] = (float)r[4]; p.vz[o] = (float)r[5];
+        check_velocity(r[3], r[4], r[5], d);
         if (ids) ids[o] = id0 + (uint32_t)i;
     }
 }
@@ -118,7 +132,9 @@ __global__ void k_soa_to_f32(Soa6 s, int64_t n, PartF32 p, uint32_t *ids, int64_
         const int64_t o = dst + i;
         p.cell[o] = pack_cell(ix, iy, iz);
         p.ox[o] = ox; p.oy[o] = oy; p.oz[o] = oz;
-        p.vx[o] = (float)s.p[3][i]; p.vy[o] = (float)s.p[4][i]; p.vz[o] = (float)s.p[5][i];
+        const double vx = s.p[3][i], vy = s.p[4][i], vz = s.p[5][i];
+        p.vx[o] = (float)vx; p.vy[o] = (float)vy; p.vz[o] = (float)vz;
+        check_velocity(vx, vy, vz, d);
         if (ids) ids[o] = id0 + (uint32_t)i;
     }
 }
@@ -215,6 +231,7 @@ void launch_tiled(ohpic_ctx *c, int mode, int strict)
     a.with_energy = c->with_energy ? 1 : 0;
     a.sorted = c->sorted ? 1 : 0;
     a.ppl = c->cfg.precision == OHPIC_FP32 && (mode == MODE_PUSH || mode == MODE_DEPOSIT) ? c->lane_particles : 2;
+    a.tma_polls = c->tma_polls;
     a.chunk = 4096;
     for (int s = 0; s < OHPIC_MAX_SPECIES; ++s) {
         a.seg[s] = c->seg[s];

@@ -19,23 +19,15 @@
 #include <math.h>
 #include <stdint.h>
 
-#include <mutex>
-
 #include "ohpic_internal.cuh"
 
 namespace ohpic {
 namespace {
 
 constexpr int64_t kNoAllocMaxNodes = (int64_t)1 << 21;   // e.g. 128^3 nodes
-constexpr int kMaxDevices = 64;
 
 // Scratch shared by every call on a device; zero at load and cleared by each call.
 static __device__ __align__(256) unsigned long long g_noalloc_sum[kNoAllocMaxNodes];
-
-// Device address of g_noalloc_sum per device, looked up once with that device current.
-std::once_flag g_once[kMaxDevices];
-void *g_addr[kMaxDevices];
-cudaError_t g_addr_err[kMaxDevices];
 
 __device__ __forceinline__ double wrap_pos(double p, int n)
 {
@@ -118,15 +110,16 @@ extern "C" int ohpic_scatter_noalloc(const double *x, const double *y, const dou
     if (weights != OHPIC_WEIGHTS_REFERENCE && weights != OHPIC_WEIGHTS_STANDARD) return OHPIC_ERR_INVALID;
     const int64_t ncell = (int64_t)nx * ny * nz;
     if (ncell > kNoAllocMaxNodes) return OHPIC_ERR_CAPACITY;   // grid larger than the static scratch
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    // The scratch array's device address in the current device's context, looked
+    // up on every call (it allocates nothing): a cached address would go stale if
+    // the caller reset the device or tore down its primary context, after which
+    // the module is loaded again and the array may move.
+    void *addr = nullptr;
+    if (cudaGetSymbolAddress(&addr, g_noalloc_sum) != cudaSuccess || !addr) {
         cudaGetLastError();
         return OHPIC_ERR_CUDA;
     }
-    // First call on this device: look up the device address of the scratch array.
-    std::call_once(g_once[dev], [dev] { g_addr_err[dev] = cudaGetSymbolAddress(&g_addr[dev], g_noalloc_sum); });
-    if (g_addr_err[dev] != cudaSuccess || !g_addr[dev]) return OHPIC_ERR_CUDA;
-    unsigned long long *sum = (unsigned long long *)g_addr[dev];
+    unsigned long long *sum = (unsigned long long *)addr;
     cudaStream_t s = (cudaStream_t)stream;
     if (n > 0) k_noalloc_deposit<<<blocks(n), 256, 0, s>>>(x, y, z, n, nx, ny, nz, weights, sum);
     k_noalloc_finish<<<blocks(ncell), 256, 0, s>>>(sum, ncell, charge, rho);

@@ -15,6 +15,7 @@
 #include <string>
 
 #include "ohpic_internal.cuh"
+#include "tma.cuh"
 
 using namespace ohpic;
 
@@ -152,6 +153,15 @@ int check_device(ohpic_ctx *c)
 
 bool species_ok(const ohpic_ctx *c, int s) { return c && s >= 0 && s < c->cfg.nspecies; }
 
+// An upload the conversion kernel flagged (a position it cannot wrap, a
+// non-finite value) leaves the species empty, so no kernel reads the bad particle.
+int check_upload(ohpic_ctx *c, int s)
+{
+    const int rc = check_device(c);
+    if (rc != OHPIC_OK) c->count[s] = 0;
+    return rc;
+}
+
 // Clears the deposit target: rho (FP64 form) or the per-species fixed-point
 // weight sums (FP32 form, turned into rho by the next solve or download).
 void zero_deposit(ohpic_ctx *c)
@@ -226,16 +236,31 @@ struct SnapHeader {
 };
 static_assert(sizeof(SnapHeader) == 256, "snapshot header is 256 bytes");
 
-// Bytes of one species' arrays: FP32 7 words + id; FP64 6 doubles + id, padded to 8.
-// A restored FP32 snapshot's cells must lie in the grid (the push relies on it).
-__global__ void k_check_cells(const int32_t *cell, int64_t n, int nx, int ny, int nz, DevDiag *d)
+// A restored FP32 snapshot must hold what the push relies on without checking:
+// cells inside the grid, offsets in [0, 1) and finite velocities.  Species
+// segment from index `seg`, n particles.
+__global__ void k_check_restored(PartF32 p, int64_t seg, int64_t n, int nx, int ny, int nz, DevDiag *d)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t c = cell[i];
-        if ((cell_x(c) >= nx || cell_y(c) >= ny || cell_z(c) >= nz) && atomicCAS(&d->err_code, 0, OHPIC_ERR_BOUNDS) == 0)
-            d->err_info = 11;
+        const int64_t k = seg + i;
+        const int32_t c = p.cell[k];
+        const float ox = p.ox[k], oy = p.oy[k], oz = p.oz[k];
+        int code = 0, info = 0;
+        if (cell_x(c) >= nx || cell_y(c) >= ny || cell_z(c) >= nz) {
+            code = OHPIC_ERR_BOUNDS;
+            info = 11;
+        } else if (!(ox >= 0.f && ox < 1.f && oy >= 0.f && oy < 1.f && oz >= 0.f && oz < 1.f)) {
+            code = isfinite(ox) && isfinite(oy) && isfinite(oz) ? OHPIC_ERR_BOUNDS : OHPIC_ERR_NONFINITE;
+            info = 14;
+        } else if (!(isfinite(p.vx[k]) && isfinite(p.vy[k]) && isfinite(p.vz[k]))) {
+            code = OHPIC_ERR_NONFINITE;
+            info = 15;
+        }
+        if (code && atomicCAS(&d->err_code, 0, code) == 0) d->err_info = info;
     }
 }
+
+// Bytes of one species' arrays: FP32 7 words + id; FP64 6 doubles + id, padded to 8.
 
 int64_t snap_species_bytes(bool f64, int64_t n)
 {
@@ -361,6 +386,7 @@ int ohpic_create(const ohpic_config *cfg, ohpic_ctx **out)
     c->sc_dt = NAN;
     c->dep_strategy = OHPIC_DEPOSIT_LANES;
     c->lane_particles = 4;
+    c->tma_polls = kTmaWaitPolls;
     Geom &g = c->g;
     if (!make_geom(k, tile, c->halo, g)) {
         ohpic_destroy(c);
@@ -471,7 +497,7 @@ int ohpic_upload_particles_soa(ohpic_ctx *c, int s, const double *x, const doubl
     c->sorted = false;
     c->rho_valid = false;
     c->kin_valid = false;
-    return check_device(c);
+    return check_upload(c, s);
 }
 
 int ohpic_upload_particles(ohpic_ctx *c, int s, const void *pbuf, int64_t n, int64_t stride)
@@ -496,7 +522,7 @@ int ohpic_upload_particles(ohpic_ctx *c, int s, const void *pbuf, int64_t n, int
     c->sorted = false;
     c->rho_valid = false;
     c->kin_valid = false;
-    return check_device(c);
+    return check_upload(c, s);
 }
 
 int ohpic_init_particles(ohpic_ctx *c, uint64_t initstate, uint64_t initseq, uint64_t advance,
@@ -661,12 +687,16 @@ int ohpic_step(ohpic_ctx *c, double dt, int nsteps)
 {
     if (!c || !std::isfinite(dt) || nsteps < 0) return fail(c, OHPIC_ERR_INVALID, "step: bad arguments");
     cudaSetDevice(c->dev);
-    if (!c->sorted && c->cfg.sort_every > 0) sort_particles(c);
+    if (!c->sorted && c->cfg.sort_every > 0) {
+        const int rc = sort_particles(c);
+        if (rc != OHPIC_OK) return rc;
+    }
     for (int i = 0; i < nsteps; ++i) {
         int rc = do_solve(c);
+        if (rc == OHPIC_OK) rc = do_push(c, dt);
+        if (rc == OHPIC_OK && c->cfg.sort_every > 0 && c->steps_since_sort >= c->cfg.sort_every)
+            rc = sort_particles(c);
         if (rc != OHPIC_OK) return rc;
-        do_push(c, dt);
-        if (c->cfg.sort_every > 0 && c->steps_since_sort >= c->cfg.sort_every) sort_particles(c);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(c, OHPIC_ERR_CUDA, std::string("step: ") + cudaGetErrorString(e));
@@ -768,6 +798,13 @@ int ohpic_set_energy_tracking(ohpic_ctx *c, int enable)
     if (!c) return OHPIC_ERR_INVALID;
     c->with_energy = enable != 0;
     c->kin_valid = false;
+    return OHPIC_OK;
+}
+
+int ohpic_set_tma_wait_limit(ohpic_ctx *c, uint32_t polls)
+{
+    if (!c) return OHPIC_ERR_INVALID;
+    c->tma_polls = polls;
     return OHPIC_OK;
 }
 
@@ -991,8 +1028,8 @@ int ohpic_snapshot_load(ohpic_ctx *c, const void *host, int64_t bytes)
         c->count[s] = n;
         if (!f64 && n > 0) {
             const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 16);
-            k_check_cells<<<(unsigned)blocks, 256, 0, c->stream>>>(c->p32[c->cur].cell + c->seg[s], n, c->cfg.nx,
-                                                                   c->cfg.ny, c->cfg.nz, c->diag);
+            k_check_restored<<<(unsigned)blocks, 256, 0, c->stream>>>(c->p32[c->cur], c->seg[s], n, c->cfg.nx,
+                                                                      c->cfg.ny, c->cfg.nz, c->diag);
         }
         p += snap_species_bytes(f64, n);
     }
@@ -1002,7 +1039,9 @@ int ohpic_snapshot_load(ohpic_ctx *c, const void *host, int64_t bytes)
         if (rc != OHPIC_OK) {
             // refuse the image and leave no particle that a kernel could misread
             for (int s = 0; s < c->cfg.nspecies; ++s) c->count[s] = 0;
-            return fail(c, OHPIC_ERR_INVALID, "snapshot_load: a particle cell lies outside the grid");
+            return fail(c, OHPIC_ERR_INVALID,
+                        "snapshot_load: a particle lies outside the grid, has an offset outside [0, 1) or a "
+                        "non-finite value (" + c->err + ")");
         }
     }
     c->steps = h.steps;

@@ -115,6 +115,7 @@ struct TileArgs {
     int with_energy;                   // accumulate kinetic energy / momentum
     int sorted;                        // tile_begin valid
     int ppl;                           // FP32 push/deposit: particles per lane, 2 or 4
+    uint32_t tma_polls;                // bound of the wait for the staged E box (0: give up at once)
     int64_t seg[OHPIC_MAX_SPECIES];
     int64_t count[OHPIC_MAX_SPECIES];
     SpeciesConst sc[OHPIC_MAX_SPECIES];
@@ -265,6 +266,7 @@ struct ohpic_ctx {
     int halo;
     int dep_strategy;           // OHPIC_DEPOSIT_* for the FP32 warp deposit
     int lane_particles;         // FP32 push/deposit: particles per lane (2 or 4)
+    uint32_t tma_polls;         // polls allowed for the staged E box (ohpic_set_tma_wait_limit)
     bool with_energy;
     bool kin_valid;             // diag->kin holds the sums of the current velocities
 

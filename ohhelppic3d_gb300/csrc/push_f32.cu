@@ -479,6 +479,15 @@ __device__ __forceinline__ int advance(const TileArgs &a, const Box &box, bool e
     return dkey;
 }
 
+// A thread whose bounded wait for the E box gave up has gathered from global
+// memory, but the copy may still be landing in this CTA's shared memory.  It
+// waits the copy out (bounded again) before the CTA can finish and release that
+// memory; a copy that never completes leaves a second error site.
+__device__ __forceinline__ void drain_tma(const TileArgs &a, bool lost, uint64_t *ebar)
+{
+    if (lost && !mbar_wait(ebar, 0, kTmaWaitPolls)) flag_error(a.diag, OHPIC_ERR_TIMEOUT, 7);
+}
+
 // Two consecutive particles per lane (8-byte vector loads and stores); the
 // pair's weights are summed in registers when both fall in one cell, then the
 // warp combines lanes sharing a cell (warp_run_deposit), a second round only
@@ -514,7 +523,8 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
         __syncthreads();
     }
     bool e_ok = box.on;
-    if (tma && !mbar_wait(ebar, 0, kTmaWaitPolls)) {
+    const bool lost = tma && !mbar_wait(ebar, 0, a.tma_polls);
+    if (lost) {
         flag_error(a.diag, OHPIC_ERR_TIMEOUT, 5);
         e_ok = false;   // gather from global memory instead
     }
@@ -562,6 +572,7 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
         cur[0] = nxt[0];
         cur[1] = nxt[1];
     }
+    drain_tma(a, lost, ebar);
     if (kDeposit && box.on) {
         __syncthreads();
         flush_f32(a, it, slo, shi);
@@ -603,7 +614,8 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
         __syncthreads();
     }
     bool e_ok = box.on;
-    if (tma && !mbar_wait(ebar, 0, kTmaWaitPolls)) {
+    const bool lost = tma && !mbar_wait(ebar, 0, a.tma_polls);
+    if (lost) {
         flag_error(a.diag, OHPIC_ERR_TIMEOUT, 6);
         e_ok = false;
     }
@@ -676,6 +688,7 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
         }
         warp_run_deposit<DEP>(acc_key, acc, slo, shi, box.sx, box.sxy);
     }
+    drain_tma(a, lost, ebar);
     if (box.on) {
         __syncthreads();
         flush_f32(a, it, slo, shi);
