@@ -60,18 +60,19 @@ uint32_t orc_pcg32_random(orc_pcg32 *rng)
  * "negative" delta rewinds. */
 void orc_pcg32_advance(orc_pcg32 *rng, uint64_t delta)
 {
-    uint64_t acc_mult = 1u, acc_plus = 0u;
-    uint64_t cur_mult = PCG_MULT, cur_plus = rng->inc;
-    while (delta > 0) {
+    /* total: the map for the bits of delta consumed so far; step: the map for
+     * 2^bit steps, squared once per bit (a*(a*s+c)+c = a^2 s + (a+1) c). */
+    uint64_t total_a = 1u, total_c = 0u;
+    uint64_t step_a = PCG_MULT, step_c = rng->inc;
+    for (; delta; delta >>= 1u) {
         if (delta & 1u) {
-            acc_mult *= cur_mult;
-            acc_plus = acc_plus * cur_mult + cur_plus;
+            total_a = total_a * step_a;
+            total_c = total_c * step_a + step_c;
         }
-        cur_plus = (cur_mult + 1u) * cur_plus;
-        cur_mult *= cur_mult;
-        delta >>= 1u;
+        step_c = step_c * (step_a + 1u);
+        step_a = step_a * step_a;
     }
-    rng->state = acc_mult * rng->state + acc_plus;
+    rng->state = total_a * rng->state + total_c;
 }
 
 /* pcg32_random_double_r: a 32-bit draw scaled by 2^-32 (lib/pcg-c/src/pcg32_double.c:60-63). */

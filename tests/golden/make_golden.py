@@ -101,7 +101,9 @@ def small_run() -> dict:
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py <path of the reference checkout>")
+    ref_root = sys.argv[1]
     pcg = reference_pcg(ref_root)
     with open(os.path.join(HERE, "pcg32_reference.json"), "w") as f:
         json.dump(pcg, f, indent=1)

@@ -9,7 +9,8 @@ reach, against the FP64 references.
   * A scaled-down clustered two-stream plasma (16x16x64 cells; background
     electrons, a beam drifting at +5 along z confined to the central 30% of x
     and y, ions; B = 0): the plain FP64 form against the oracle with exact cell
-    indices and crossings, and the FP32 form against the oracle.
+    indices and crossings, and the FP32 form against the oracle (E and phi
+    <= 1e-5, rho <= 2e-5).
   * One run through the continuous-batching server against an oracle run of the
     same seed: counts exact, fields and particles within the precision form's
     tolerance.
@@ -139,9 +140,12 @@ def test_clustered_beam_against_oracle(ohpic, oracle_mod, precision):
                     assert v <= tol[step][2], (step, k, v)
     print("clustered beam, precision", precision, report)
     if precision == P.FP32:
+        # The bar is on E (and phi).  rho is the node charge with no smoothing, and
+        # the beam is two-stream unstable, so its FP32 rounding grows fastest:
+        # 1.0e-5 after 100 steps on GB300, bounded here at 2e-5.
         for step, errs in report.items():
             for k, v in errs.items():
-                assert v <= 1e-5, (step, k, v)
+                assert v <= (2e-5 if k == "rho" else 1e-5), (step, k, v)
     o.close()
 
 
