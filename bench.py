@@ -14,8 +14,9 @@ compared with the FP64 run's from the same seeds (`accuracy`).  The FP32 form in
 the reference's own swapped-weight convention is run the same way beside it,
 with its own error.  Also in the line: the 32^3 configuration's errors against
 the oracle itself (`c3_vs_oracle`), the clustered two-stream workload (`c4`),
-both forms end to end through the C ABI (`e2e`), the oracle on the host cores
-(`cpu_baseline`) and the serving ensemble (`serving`).
+the bounded-domain field solve at 256^3 (`poisson_bounded`), both forms end to
+end through the C ABI (`e2e`), the oracle on the host cores (`cpu_baseline`)
+and the serving ensemble (`serving`).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--workload c2|c1|c4] [--forms fp32,fp64] [--weights 1|0] [--no-e2e] ...
@@ -450,6 +451,40 @@ def c3_vs_oracle(P, weights_list, threads: int) -> dict:
     return out
 
 
+def run_poisson_bc(P, torch, peak, n=(256, 256, 256), reps: int = 10) -> dict:
+    """The bounded-domain field solve (non-periodic kinds) at 256^3, FP64, on
+    device arrays: CUDA-event time per solve (after 3 untimed) for all-Dirichlet
+    walls and for a mixed set, with the algorithmic bytes rho read + phi write + E
+    write = 40 B per node (the transforms' internal passes count against it)."""
+    out = {"grid": list(n), "bytes_per_node": 40, "reps": reps}
+    dev = torch.device("cuda", torch.cuda.current_device())
+    shape = (n[2] + 1, n[1] + 1, n[0] + 1)
+    g = torch.Generator(device=dev).manual_seed(3)
+    rho = torch.randn(shape, dtype=torch.float64, device=dev, generator=g)
+    phi = torch.empty_like(rho)
+    e = torch.empty((3,) + shape, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    nodes = shape[0] * shape[1] * shape[2]
+    for name, kinds in (("dirichlet_xyz", (P.BC_DIRICHLET,) * 3),
+                        ("dirichlet_neumann_periodic", (P.BC_DIRICHLET, P.BC_NEUMANN, P.BC_PERIODIC))):
+        with P.PoissonSolver(n, kinds, table=P.TABLE_CORRECTED) as s:
+            for _ in range(3):
+                s.solve_device(rho.data_ptr(), phi.data_ptr(), e.data_ptr(), stream.cuda_stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(reps):
+                s.solve_device(rho.data_ptr(), phi.data_ptr(), e.data_ptr(), stream.cuda_stream)
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+        gbs = 40.0 * nodes / (ms / 1e3) / 1e9
+        out[name] = {"kinds": list(kinds), "ms_per_solve": ms, "achieved_gbs": gbs, "frac": gbs / peak[0]}
+    del rho, phi, e
+    torch.cuda.empty_cache()
+    return out
+
+
 def accuracy_block(caps32: dict, caps64: dict, weights: int) -> dict:
     steps = {str(k): compare(caps32[k], caps64[k]) for k in CHECKPOINTS}
     e100 = steps[str(CHECKPOINTS[-1])]["e"]
@@ -637,6 +672,7 @@ def main(argv=None) -> int:
                     help="skip the FP32 run in the other CIC convention")
     ap.add_argument("--no-c3", action="store_true", help="skip the 32^3 errors against the oracle")
     ap.add_argument("--no-c4", action="store_true", help="skip the clustered two-stream block")
+    ap.add_argument("--no-bounded", action="store_true", help="skip the bounded-domain field solve timing")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n", default=None, help="grid override nx,ny,nz (same physics and ppc; for profiling)")
@@ -730,6 +766,10 @@ def main(argv=None) -> int:
         torch.cuda.empty_cache()
         c4 = dict(_short(res), workload=w4.description)
 
+    bounded = None
+    if args.workload == "c2" and not args.no_bounded and not args.n:
+        bounded = run_poisson_bc(P, torch, peak)
+
     cpu = None
     if solo and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -777,6 +817,8 @@ def main(argv=None) -> int:
         line["c3_vs_oracle"] = c3
     if c4 is not None:
         line["c4"] = c4
+    if bounded is not None:
+        line["poisson_bounded"] = bounded
     if serving is not None:
         line["serving"] = serving
     if dist.rank == 0:

@@ -279,6 +279,48 @@ int ohpic_stats(ohpic_ctx *ctx, int64_t *launches, int64_t *push_launches, doubl
 /* Device bytes held by the context. */
 int ohpic_memory(ohpic_ctx *ctx, int64_t *device_bytes);
 
+/* Field solve on a bounded block with a boundary kind per axis: the reference's
+ * t_PoissonFieldSolver with non-periodic kinds for one rank
+ * (src/field_solver/poisson_field_solver.f90:34-175 over
+ * src/field_solver/poisson/poisson_solver3d.f90:28-207 and the FFTW r2r kinds,
+ * logical ranges and normalisers of src/field_solver/fft/fftw3/mpi_fftw3_solver.f90:151-236).
+ * The block is the reference's global block: nodes 0..n[d] on every axis,
+ * (n[0]+1)(n[1]+1)(n[2]+1) doubles with x fastest.  Kinds follow
+ * src/field_solver/field_boundary_type.f90:21-71; boundary_values is the
+ * reference's boundary_values(2,3) (lo_x, hi_x, lo_y, hi_y, lo_z, hi_z; null = 0).
+ *
+ * OHPIC_TABLE_AS_WRITTEN reproduces the reference: it divides by the sum of the
+ * squared per-axis wave numbers indexed by global node (poisson_solver3d.f90:62-78,
+ * whose Dirichlet and Neumann entries are eigenvalues 2(cos t - 1), so their
+ * squares are not Laplacian eigenvalues), adds the wall terms of :81-102 to the
+ * block's first and last node planes (a Dirichlet wall's plane is outside the
+ * transform, so its value has no effect), and zeroes element (0,0,0) of the
+ * block when every logical range starts at node 0.  OHPIC_TABLE_CORRECTED divides
+ * by the discrete Laplacian's own eigenvalues (sum_d 2 - 2 cos theta_d; periodic
+ * axes as written), zeroes only a null mode, takes a Dirichlet value as the wall
+ * potential (entering the adjacent interior node) and a Neumann value as the
+ * reference's pure-Neumann term (2 bv low, -2 bv high).  Both solve
+ * -laplacian(phi) = rho with dx = 1 and use the reference's pi literal.
+ * Outside the transformed range, phi holds a periodic axis' image of node 0 at
+ * node n and a Dirichlet wall's potential (0 as written).  e (nullable) receives
+ * three such blocks, E = -grad phi by the reference's central difference (one-sided
+ * at the walls of non-periodic axes).  Grids: n[d] >= 1 (>= 2 for Dirichlet),
+ * at most 4096. */
+enum { OHPIC_BC_PERIODIC = 0, OHPIC_BC_DIRICHLET = 1, OHPIC_BC_NEUMANN = 2, OHPIC_BC_DIRICHLET_NEUMANN = 3,
+       OHPIC_BC_NEUMANN_DIRICHLET = 4 };
+enum { OHPIC_TABLE_AS_WRITTEN = 0, OHPIC_TABLE_CORRECTED = 1 };
+typedef struct ohpic_poisson ohpic_poisson;
+/* Replaces new_PoissonFieldSolver (poisson_field_solver.f90:34-88). */
+int ohpic_poisson_create(const int32_t n[3], const int32_t kinds[3], const double boundary_values[6],
+                         int32_t table, int32_t device, ohpic_poisson **out);
+int ohpic_poisson_destroy(ohpic_poisson *solver);
+/* t_FieldSolver%solve (poisson_field_solver.f90:90-175) on host arrays; synchronous. */
+int ohpic_poisson_solve(ohpic_poisson *solver, const double *rho, double *phi, double *e);
+/* The same on device arrays, ordered on `stream` (a cudaStream_t; null = the
+ * solver's own stream); returns without synchronising. */
+int ohpic_poisson_solve_device(ohpic_poisson *solver, const double *rho, double *phi, double *e, void *stream);
+int ohpic_poisson_last_error(const ohpic_poisson *solver, char *buf, size_t len);
+
 /* CIC deposit that allocates no device memory (no counterpart in the reference).
  * For callers that cannot let a library allocate GPU memory, e.g. codes that size
  * all device memory once through their own pool and treat a later cudaMalloc as an

@@ -136,7 +136,16 @@ SIGNATURES = {
     "ohpic_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "ohpic_scatter_noalloc": (C.c_int, [_P, _P, _P, C.c_int64, C.c_double, C.c_int32, C.c_int32, C.c_int32,
                                         C.c_int32, _P, _P]),
+    "ohpic_poisson_create": (C.c_int, [C.POINTER(C.c_int32), C.POINTER(C.c_int32), _DP, C.c_int32, C.c_int32,
+                                       C.POINTER(_P)]),
+    "ohpic_poisson_destroy": (C.c_int, [_P]),
+    "ohpic_poisson_solve": (C.c_int, [_P, _DP, _DP, _DP]),
+    "ohpic_poisson_solve_device": (C.c_int, [_P, _P, _P, _P, _P]),
+    "ohpic_poisson_last_error": (C.c_int, [_P, C.c_char_p, C.c_size_t]),
 }
+
+BC_PERIODIC, BC_DIRICHLET, BC_NEUMANN, BC_DIRICHLET_NEUMANN, BC_NEUMANN_DIRICHLET = range(5)
+TABLE_AS_WRITTEN, TABLE_CORRECTED = 0, 1
 
 
 def build(force: bool = False) -> str:
@@ -406,6 +415,60 @@ class PicContext:
         v = C.c_int64()
         self._check(lib().ohpic_memory(self.ptr, C.byref(v)))
         return v.value
+
+
+class PoissonSolver:
+    """The field solve on a bounded block (ohpic_poisson_*): t_PoissonFieldSolver
+    with a boundary kind per axis (poisson_field_solver.f90:34-175).  Arrays are
+    (nz+1, ny+1, nx+1) blocks of nodes, x fastest."""
+
+    def __init__(self, n, kinds, boundary_values=(0.0,) * 6, table=TABLE_AS_WRITTEN, device=0):
+        self.n = tuple(int(v) for v in n)
+        na = (C.c_int32 * 3)(*self.n)
+        ka = (C.c_int32 * 3)(*[int(k) for k in kinds])
+        bv = np.ascontiguousarray(boundary_values, dtype=np.float64)
+        ptr = _P()
+        rc = lib().ohpic_poisson_create(na, ka, _dp(bv), int(table), int(device), C.byref(ptr))
+        if rc != OK:
+            raise OhpicError(rc, lib().ohpic_status_string(rc).decode())
+        self.ptr = ptr
+
+    def _check(self, rc: int):
+        if rc != OK:
+            buf = C.create_string_buffer(512)
+            lib().ohpic_poisson_last_error(self.ptr, buf, 512)
+            raise OhpicError(rc, buf.value.decode(errors="replace"))
+
+    def solve(self, rho: np.ndarray, with_e: bool = True):
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        shape = (self.n[2] + 1, self.n[1] + 1, self.n[0] + 1)
+        if rho.shape != shape:
+            raise OhpicError(ERR_INVALID, f"rho must have shape {shape}")
+        phi = np.empty_like(rho)
+        e = np.empty((3,) + shape) if with_e else None
+        self._check(lib().ohpic_poisson_solve(self.ptr, _dp(rho), _dp(phi), _dp(e) if e is not None else None))
+        return (phi, e) if with_e else phi
+
+    def solve_device(self, rho_ptr: int, phi_ptr: int, e_ptr: int | None = None, stream: int | None = None):
+        self._check(lib().ohpic_poisson_solve_device(self.ptr, _P(rho_ptr), _P(phi_ptr),
+                                                     _P(e_ptr) if e_ptr else None, _P(stream) if stream else None))
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            lib().ohpic_poisson_destroy(self.ptr)
+            self.ptr = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------------------

@@ -103,6 +103,9 @@ def lib():
         L.orc_green.restype = C.c_double
         L.orc_green.argtypes = [C.c_int] * 6
         L.orc_pcg32_fill.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, C.POINTER(C.c_uint32), C.c_int64]
+        L.orc_poisson_bc.restype = C.c_int
+        L.orc_poisson_bc.argtypes = [C.POINTER(C.c_int)] * 2 + [dp, C.c_int, dp, dp, dp]
+        L.orc_r2r_1d.argtypes = [C.c_int, dp, dp, C.c_int]
         _lib = L
     return _lib
 
@@ -153,6 +156,34 @@ class Setup:
         for d in range(3):
             vol *= max(min(hi[d], self.n[d]) - max(lo[d], 0.0), 0.0)
         return int(sp.ppc * vol)
+
+
+BC_PERIODIC, BC_DIRICHLET, BC_NEUMANN, BC_DIRICHLET_NEUMANN, BC_NEUMANN_DIRICHLET = range(5)
+R2HC, HC2R, RODFT00, REDFT00, RODFT01, RODFT10, REDFT01, REDFT10 = range(8)
+
+
+def r2r_1d(kind: int, x) -> np.ndarray:
+    """One unnormalised FFTW-convention real transform by its defining sum."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.empty_like(x)
+    lib().orc_r2r_1d(kind, _dp(x), _dp(y), len(x))
+    return y
+
+
+def poisson_bc(rho: np.ndarray, kinds, bv=(0.0,) * 6, corrected: bool = False, with_e: bool = True):
+    """The bounded-domain field solve on a (nz+1, ny+1, nx+1) block of nodes
+    (x fastest): returns phi (and E as (3, nz+1, ny+1, nx+1))."""
+    rho = np.ascontiguousarray(rho, dtype=np.float64)
+    n = (C.c_int * 3)(rho.shape[2] - 1, rho.shape[1] - 1, rho.shape[0] - 1)
+    k = (C.c_int * 3)(*[int(v) for v in kinds])
+    b = np.ascontiguousarray(bv, dtype=np.float64)
+    phi = np.empty_like(rho)
+    e = np.empty((3,) + rho.shape) if with_e else None
+    rc = lib().orc_poisson_bc(n, k, _dp(b), int(bool(corrected)), _dp(rho), _dp(phi),
+                              _dp(e) if e is not None else None)
+    if rc != 0:
+        raise ValueError("orc_poisson_bc: bad grid or kinds")
+    return (phi, e) if with_e else phi
 
 
 def pcg32_draws(initstate: int, initseq: int, n: int, advance: int = 0) -> np.ndarray:

@@ -729,3 +729,297 @@ void orc_diagnostics(orc_sim *s, orc_diag *d)
     d->momentum[2] = mz;
     for (int a = 0; a < 3; ++a) d->crossings[a] = s->crossings[a];
 }
+
+/* ------------------------------------------------------------------------ */
+/* Bounded-domain field solve (non-periodic kinds).  The restatement follows  */
+/* the reference's own algorithm: FFTW's r2r transforms per axis (written     */
+/* here as their defining sums), the logical ranges and normalisers of        */
+/* mpi_fftw3_solver.f90:151-207, the table and wall terms of                  */
+/* poisson_solver3d.f90:56-132 and the solve of :134-207.                      */
+/* ------------------------------------------------------------------------ */
+enum { R2R_R2HC = 0, R2R_HC2R, R2R_RODFT00, R2R_REDFT00, R2R_RODFT01, R2R_RODFT10, R2R_REDFT01, R2R_REDFT10 };
+
+/* sin and cos of pi * a / b with the integer numerator reduced modulo 2b first
+ * (exact pi, like FFTW's own twiddles). */
+static double sinpi_frac(int64_t a, int64_t b)
+{
+    a %= 2 * b;
+    if (a < 0) a += 2 * b;
+    return sin(TWO_PI_EXACT * 0.5 * (double)a / (double)b);
+}
+static double cospi_frac(int64_t a, int64_t b)
+{
+    a %= 2 * b;
+    if (a < 0) a += 2 * b;
+    return cos(TWO_PI_EXACT * 0.5 * (double)a / (double)b);
+}
+
+void orc_r2r_1d(int kind, const double *x, double *y, int N)
+{
+    switch (kind) {
+    case R2R_R2HC:   /* r_k = sum x_j cos(2 pi jk/N), i_k = -sum x_j sin(2 pi jk/N), y[N-k] = i_k */
+        for (int k = 0; k <= N / 2; ++k) {
+            double re = 0.0, im = 0.0;
+            for (int j = 0; j < N; ++j) {
+                re += x[j] * cospi_frac(2 * (int64_t)j * k, N);
+                im -= x[j] * sinpi_frac(2 * (int64_t)j * k, N);
+            }
+            y[k] = re;
+            if (k > 0 && 2 * k != N) y[N - k] = im;
+        }
+        break;
+    case R2R_HC2R:   /* x_j = r_0 + sum_k 2 (r_k cos - i_k sin) + r_{N/2} (-1)^j */
+        for (int j = 0; j < N; ++j) {
+            double s = x[0];
+            for (int k = 1; 2 * k < N; ++k)
+                s += 2.0 * (x[k] * cospi_frac(2 * (int64_t)j * k, N) - x[N - k] * sinpi_frac(2 * (int64_t)j * k, N));
+            if (N % 2 == 0) s += (j % 2 ? -1.0 : 1.0) * x[N / 2];
+            y[j] = s;
+        }
+        break;
+    case R2R_RODFT00:   /* DST-I: 2 sum x_j sin(pi (j+1)(k+1)/(N+1)) */
+        for (int k = 0; k < N; ++k) {
+            double s = 0.0;
+            for (int j = 0; j < N; ++j) s += x[j] * sinpi_frac((int64_t)(j + 1) * (k + 1), N + 1);
+            y[k] = 2.0 * s;
+        }
+        break;
+    case R2R_REDFT00:   /* DCT-I: x_0 + (-1)^k x_{N-1} + 2 sum_{j=1}^{N-2} x_j cos(pi jk/(N-1)) */
+        for (int k = 0; k < N; ++k) {
+            double s = 0.0;
+            for (int j = 1; j < N - 1; ++j) s += x[j] * cospi_frac((int64_t)j * k, N - 1);
+            y[k] = x[0] + (k % 2 ? -1.0 : 1.0) * x[N - 1] + 2.0 * s;
+        }
+        break;
+    case R2R_RODFT01:   /* DST-III: (-1)^k x_{N-1} + 2 sum_{j=0}^{N-2} x_j sin(pi (j+1)(2k+1)/(2N)) */
+        for (int k = 0; k < N; ++k) {
+            double s = 0.0;
+            for (int j = 0; j < N - 1; ++j) s += x[j] * sinpi_frac((int64_t)(j + 1) * (2 * k + 1), 2 * N);
+            y[k] = (k % 2 ? -1.0 : 1.0) * x[N - 1] + 2.0 * s;
+        }
+        break;
+    case R2R_RODFT10:   /* DST-II: 2 sum x_j sin(pi (2j+1)(k+1)/(2N)) */
+        for (int k = 0; k < N; ++k) {
+            double s = 0.0;
+            for (int j = 0; j < N; ++j) s += x[j] * sinpi_frac((int64_t)(2 * j + 1) * (k + 1), 2 * N);
+            y[k] = 2.0 * s;
+        }
+        break;
+    case R2R_REDFT01:   /* DCT-III: x_0 + 2 sum_{j=1}^{N-1} x_j cos(pi j(2k+1)/(2N)) */
+        for (int k = 0; k < N; ++k) {
+            double s = 0.0;
+            for (int j = 1; j < N; ++j) s += x[j] * cospi_frac((int64_t)j * (2 * k + 1), 2 * N);
+            y[k] = x[0] + 2.0 * s;
+        }
+        break;
+    case R2R_REDFT10:   /* DCT-II: 2 sum x_j cos(pi (2j+1)k/(2N)) */
+        for (int k = 0; k < N; ++k) {
+            double s = 0.0;
+            for (int j = 0; j < N; ++j) s += x[j] * cospi_frac((int64_t)(2 * j + 1) * k, 2 * N);
+            y[k] = 2.0 * s;
+        }
+        break;
+    default:
+        break;
+    }
+}
+
+/* convert_fft_type (mpi_fftw3_solver.f90:151-207) for the global block 0..n. */
+typedef struct {
+    int fwd, bwd, ls, L;
+    double norm;
+} bc_axis;
+
+static int bc_axis_of(int kind, int n, bc_axis *a)
+{
+    switch (kind) {
+    case ORC_BC_PERIODIC: a->fwd = R2R_R2HC; a->bwd = R2R_HC2R; a->ls = 0; a->L = n; a->norm = (double)a->L; break;
+    case ORC_BC_DIRICHLET: a->fwd = a->bwd = R2R_RODFT00; a->ls = 1; a->L = n - 1; a->norm = 2.0 * (a->L + 1.0); break;
+    case ORC_BC_NEUMANN: a->fwd = a->bwd = R2R_REDFT00; a->ls = 0; a->L = n + 1; a->norm = 2.0 * (a->L - 1.0); break;
+    case ORC_BC_DIRICHLET_NEUMANN: a->fwd = R2R_RODFT01; a->bwd = R2R_RODFT10; a->ls = 1; a->L = n; a->norm = 2.0 * a->L; break;
+    case ORC_BC_NEUMANN_DIRICHLET: a->fwd = R2R_REDFT01; a->bwd = R2R_REDFT10; a->ls = 0; a->L = n; a->norm = 2.0 * a->L; break;
+    default: return -1;
+    }
+    return a->L >= 1 && !(kind == ORC_BC_NEUMANN && a->L < 2) ? 0 : -1;
+}
+
+/* calc_wave_number (poisson_solver3d.f90:104-132) with the reference's pi. */
+static double bc_wave_number(int k, int n, int kind)
+{
+    switch (kind) {
+    case ORC_BC_PERIODIC:
+        if (k <= n / 2) return 2.0 * sin(REF_PI * k / (double)n);
+        return 2.0 * sin(REF_PI * (n - k) / (double)n);
+    case ORC_BC_DIRICHLET: return 2.0 * (cos(REF_PI * (k + 1) / (double)(n + 1)) - 1.0);
+    case ORC_BC_NEUMANN: return 2.0 * (cos(REF_PI * k / (double)n) - 1.0);
+    case ORC_BC_DIRICHLET_NEUMANN:
+    case ORC_BC_NEUMANN_DIRICHLET: return 2.0 * (cos(REF_PI * (k + 0.5) / (double)(n + 1)) - 1.0);
+    }
+    return 0.0;
+}
+
+/* The Laplacian's eigenvalue (negated) of logical mode i of each kind. */
+static double bc_eigenvalue(int i, int n, int kind)
+{
+    switch (kind) {
+    case ORC_BC_PERIODIC: {
+        const double w = bc_wave_number(i, n, kind);
+        return w * w;
+    }
+    case ORC_BC_DIRICHLET: return 2.0 - 2.0 * cos(REF_PI * (i + 1) / (double)n);
+    case ORC_BC_NEUMANN: return 2.0 - 2.0 * cos(REF_PI * i / (double)n);
+    case ORC_BC_DIRICHLET_NEUMANN:
+    case ORC_BC_NEUMANN_DIRICHLET: return 2.0 - 2.0 * cos(REF_PI * (i + 0.5) / (double)n);
+    }
+    return 0.0;
+}
+
+/* calc_boundary_term (poisson_solver3d.f90:81-102). */
+static void bc_terms(int kind, const double bv[2], double t[2])
+{
+    switch (kind) {
+    case ORC_BC_PERIODIC: t[0] = bv[0]; t[1] = bv[1]; break;
+    case ORC_BC_DIRICHLET: t[0] = -bv[0]; t[1] = -bv[1]; break;
+    case ORC_BC_NEUMANN: t[0] = 2.0 * bv[0]; t[1] = -2.0 * bv[1]; break;
+    default: t[0] = -bv[0]; t[1] = -2.0 * bv[1]; break;   /* both mixed kinds */
+    }
+}
+
+static int bc_has_wall_lo(int kind) { return kind == ORC_BC_DIRICHLET || kind == ORC_BC_DIRICHLET_NEUMANN; }
+static int bc_has_wall_hi(int kind) { return kind == ORC_BC_DIRICHLET || kind == ORC_BC_NEUMANN_DIRICHLET; }
+
+/* Applies one 1-D transform along `axis` of a (L0, L1, L2) array, x fastest. */
+static void bc_transform_axis(double *a, const int L[3], int axis, int kind)
+{
+    const int64_t s[3] = {1, L[0], (int64_t)L[0] * L[1]};
+    const int o1 = axis == 0 ? 1 : 0, o2 = axis == 2 ? 1 : 2;
+    const int N = L[axis];
+    double *x = (double *)malloc(sizeof(double) * N), *y = (double *)malloc(sizeof(double) * N);
+    for (int q = 0; q < L[o2]; ++q)
+        for (int p = 0; p < L[o1]; ++p) {
+            const int64_t base = p * s[o1] + q * s[o2];
+            for (int j = 0; j < N; ++j) x[j] = a[base + j * s[axis]];
+            orc_r2r_1d(kind, x, y, N);
+            for (int j = 0; j < N; ++j) a[base + j * s[axis]] = y[j];
+        }
+    free(x);
+    free(y);
+}
+
+int orc_poisson_bc(const int n[3], const int kinds[3], const double bv[6], int corrected, const double *rho,
+                   double *phi, double *e)
+{
+    bc_axis ax[3];
+    for (int d = 0; d < 3; ++d)
+        if (n[d] < 1 || bc_axis_of(kinds[d], n[d], &ax[d]) != 0) return -1;
+    const int B[3] = {n[0] + 1, n[1] + 1, n[2] + 1};
+    const int64_t nb = (int64_t)B[0] * B[1] * B[2];
+    double *w = (double *)malloc(sizeof(double) * nb);
+    memcpy(w, rho, sizeof(double) * nb);   /* phi = rho (poisson_solver3d.f90:147) */
+#define BIDX(i, j, k) ((i) + (int64_t)B[0] * ((j) + (int64_t)B[1] * (k)))
+    for (int d = 0; d < 3; ++d) {
+        double t[2];
+        int lo = 0, hi = n[d];
+        bc_terms(kinds[d], bv + 2 * d, t);
+        if (corrected) {
+            /* A Dirichlet wall value is the wall's potential: it enters the
+             * equation of the adjacent interior node.  A Neumann value keeps the
+             * reference's meaning (2 bv at the low wall, -2 bv at the high one). */
+            if (kinds[d] == ORC_BC_PERIODIC) continue;
+            if (bc_has_wall_lo(kinds[d])) { t[0] = bv[2 * d]; lo = 1; }
+            else t[0] = 2.0 * bv[2 * d];
+            if (bc_has_wall_hi(kinds[d])) { t[1] = bv[2 * d + 1]; hi = n[d] - 1; }
+            else t[1] = -2.0 * bv[2 * d + 1];
+        }
+        /* the face planes of the block (poisson_solver3d.f90:156-168) */
+        for (int k = 0; k < B[2]; ++k)
+            for (int j = 0; j < B[1]; ++j)
+                for (int i = 0; i < B[0]; ++i) {
+                    const int g = d == 0 ? i : d == 1 ? j : k;
+                    if (g == lo) w[BIDX(i, j, k)] += t[0];
+                    if (g == hi) w[BIDX(i, j, k)] += t[1];
+                }
+    }
+    const int L[3] = {ax[0].L, ax[1].L, ax[2].L};
+    const int64_t nl = (int64_t)L[0] * L[1] * L[2];
+    double *a = (double *)malloc(sizeof(double) * nl);
+    for (int k = 0; k < L[2]; ++k)
+        for (int j = 0; j < L[1]; ++j)
+            for (int i = 0; i < L[0]; ++i)
+                a[i + (int64_t)L[0] * (j + (int64_t)L[1] * k)] = w[BIDX(i + ax[0].ls, j + ax[1].ls, k + ax[2].ls)];
+    for (int d = 0; d < 3; ++d) bc_transform_axis(a, L, d, ax[d].fwd);
+    for (int k = 0; k < L[2]; ++k)
+        for (int j = 0; j < L[1]; ++j)
+            for (int i = 0; i < L[0]; ++i) {
+                const int64_t at = i + (int64_t)L[0] * (j + (int64_t)L[1] * k);
+                double den;
+                if (corrected) {
+                    den = bc_eigenvalue(i, n[0], kinds[0]) + bc_eigenvalue(j, n[1], kinds[1]) +
+                          bc_eigenvalue(k, n[2], kinds[2]);
+                    a[at] = den == 0.0 ? 0.0 : a[at] / den;
+                } else {
+                    /* modified_wave_number at the element's global index (:62-78) */
+                    const double wx = bc_wave_number(i + ax[0].ls, n[0], kinds[0]);
+                    const double wy = bc_wave_number(j + ax[1].ls, n[1], kinds[1]);
+                    const double wz = bc_wave_number(k + ax[2].ls, n[2], kinds[2]);
+                    den = wx * wx + wy * wy + wz * wz;
+                    a[at] = a[at] / den;
+                }
+            }
+    /* element (0,0,0) of the block (:194-198): inside the transform only when
+     * every logical range starts at node 0 */
+    if (!corrected && ax[0].ls == 0 && ax[1].ls == 0 && ax[2].ls == 0) a[0] = 0.0;
+    for (int d = 2; d >= 0; --d) bc_transform_axis(a, L, d, ax[d].bwd);
+    const double norm = ax[0].norm * ax[1].norm * ax[2].norm;
+    for (int k = 0; k < B[2]; ++k)
+        for (int j = 0; j < B[1]; ++j)
+            for (int i = 0; i < B[0]; ++i) {
+                int g[3] = {i, j, k};
+                double wall = 0.0;
+                int at_wall = 0;
+                for (int d = 0; d < 3 && !at_wall; ++d) {
+                    if (kinds[d] == ORC_BC_PERIODIC && g[d] == n[d]) g[d] = 0;
+                    else if (bc_has_wall_lo(kinds[d]) && g[d] == 0) { at_wall = 1; wall = corrected ? bv[2 * d] : 0.0; }
+                    else if (bc_has_wall_hi(kinds[d]) && g[d] == n[d]) { at_wall = 1; wall = corrected ? bv[2 * d + 1] : 0.0; }
+                }
+                double v = wall;
+                if (!at_wall) {
+                    const int64_t at = (g[0] - ax[0].ls) + (int64_t)L[0] * ((g[1] - ax[1].ls) + (int64_t)L[1] * (g[2] - ax[2].ls));
+                    v = a[at] / norm;
+                }
+                phi[BIDX(i, j, k)] = v;
+            }
+    if (e) {
+        for (int k = 0; k < B[2]; ++k)
+            for (int j = 0; j < B[1]; ++j)
+                for (int i = 0; i < B[0]; ++i) {
+                    const int g[3] = {i, j, k};
+                    for (int d = 0; d < 3; ++d) {
+                        int gm[3] = {i, j, k}, gp[3] = {i, j, k};
+                        double v;
+                        const double p0 = phi[BIDX(i, j, k)];
+                        if (kinds[d] == ORC_BC_PERIODIC) {
+                            const int c = g[d] == n[d] ? 0 : g[d];
+                            gm[d] = (c + n[d] - 1) % n[d];
+                            gp[d] = (c + 1) % n[d];
+                            v = 0.5 * ((phi[BIDX(gm[0], gm[1], gm[2])] - p0) + (p0 - phi[BIDX(gp[0], gp[1], gp[2])]));
+                        } else if (g[d] == 0) {
+                            gp[d] = 1;
+                            v = p0 - phi[BIDX(gp[0], gp[1], gp[2])];
+                        } else if (g[d] == n[d]) {
+                            gm[d] = n[d] - 1;
+                            v = phi[BIDX(gm[0], gm[1], gm[2])] - p0;
+                        } else {
+                            gm[d] = g[d] - 1;
+                            gp[d] = g[d] + 1;
+                            v = 0.5 * ((phi[BIDX(gm[0], gm[1], gm[2])] - p0) + (p0 - phi[BIDX(gp[0], gp[1], gp[2])]));
+                        }
+                        e[(int64_t)d * nb + BIDX(i, j, k)] = v;
+                    }
+                }
+    }
+#undef BIDX
+    free(a);
+    free(w);
+    return 0;
+}

@@ -134,6 +134,40 @@ void orc_fft3d(double *data, int nx, int ny, int nz, int sign);
  * (poisson_solver3d.f90:104-117); returns 0 for k = 0. */
 double orc_green(int kx, int ky, int kz, int nx, int ny, int nz);
 
+/* Field solve on a bounded block with per-axis boundary kinds: the reference's
+ * poissonSolver3d_solve (src/field_solver/poisson/poisson_solver3d.f90:134-207)
+ * over the FFTW r2r transforms of src/field_solver/fft/fftw3/mpi_fftw3_solver.f90
+ * (kinds, logical ranges and normalisers :151-207, backward normalisation :235),
+ * the wave-number table of poisson_solver3d.f90:56-78,104-132 and the wall terms
+ * of :81-102, for one rank whose block is the global block 0..n per axis.
+ *
+ * Kinds (src/field_solver/field_boundary_type.f90:21-71): */
+enum { ORC_BC_PERIODIC = 0, ORC_BC_DIRICHLET = 1, ORC_BC_NEUMANN = 2, ORC_BC_DIRICHLET_NEUMANN = 3,
+       ORC_BC_NEUMANN_DIRICHLET = 4 };
+/* rho, phi: (n[0]+1)(n[1]+1)(n[2]+1) doubles, x fastest, nodes 0..n per axis.
+ * bv: boundary_values(2,3) in Fortran order (lo_x, hi_x, lo_y, hi_y, lo_z, hi_z).
+ * corrected = 0 follows the reference as written: the table is the sum of the
+ * squared per-axis wave numbers indexed by global node, the wall terms go to the
+ * block's first and last node planes, and element (0,0,0) of the block is zeroed
+ * when every logical range starts at node 0.  corrected = 1 divides by the
+ * Laplacian's own eigenvalues at the logical index (sum_d 2 - 2 cos(theta_d); the
+ * periodic axes keep (2 sin(pi k/n))^2), zeroes only a null mode, takes a
+ * Dirichlet wall value as the wall's potential (its term goes to the adjacent
+ * interior node), a Neumann value as in the reference's pure-Neumann terms (2 bv
+ * at a low wall, -2 bv at a high one) on either mixed kind, and no term on a
+ * periodic axis.  phi at nodes outside the transformed range: a periodic axis'
+ * node n is the image of node 0; a Dirichlet wall holds 0 (as written) or its
+ * value (corrected).  e (nullable): 3 blocks of the same size, E = -grad phi by
+ * the reference's central difference 0.5*((phi[i-1] - phi[i]) + (phi[i] -
+ * phi[i+1])), wrapped on periodic axes, one-sided (phi[0] - phi[1], phi[n-1] -
+ * phi[n]) at the walls of the others.  Returns 0, or -1 for bad arguments. */
+int orc_poisson_bc(const int n[3], const int kinds[3], const double bv[6], int corrected, const double *rho,
+                   double *phi, double *e);
+/* One-dimensional unnormalised real transform by its defining sum, FFTW's
+ * conventions: kind 0 R2HC, 1 HC2R, 2 RODFT00, 3 REDFT00, 4 RODFT01, 5 RODFT10,
+ * 6 REDFT01, 7 REDFT10. */
+void orc_r2r_1d(int kind, const double *x, double *y, int n);
+
 #ifdef __cplusplus
 }
 #endif
