@@ -209,8 +209,8 @@ int ohpic_download_field_ohfield(ohpic_ctx *ctx, int which, double *values, int 
  * 52 bytes, padded to 8).  The header holds the grid, form, species count, the
  * per-species counts and the step counters; the physics (qm, q, B0, dt) comes
  * from the restoring context's own config.  After a restore the next step
- * deposits the restored particles again, so an FP32 run continues bit-identically
- * (its deposit is integer); an FP64 run continues within FP64 atomic rounding.
+ * deposits the restored particles again, so a run continues bit-identically in
+ * either form (both deposits are integer fixed point).
  * ohpic_snapshot_load() requires the same grid, form and species count, and
  * counts within the context's capacities. */
 int ohpic_snapshot_size(ohpic_ctx *ctx, int64_t *bytes);
@@ -316,8 +316,8 @@ int ohpic_poisson_create(const int32_t n[3], const int32_t kinds[3], const doubl
 int ohpic_poisson_destroy(ohpic_poisson *solver);
 /* t_FieldSolver%solve (poisson_field_solver.f90:90-175) on host arrays; synchronous. */
 int ohpic_poisson_solve(ohpic_poisson *solver, const double *rho, double *phi, double *e);
-/* The same on device arrays, ordered on `stream` (a cudaStream_t; null = the
- * solver's own stream); returns without synchronising. */
+/* The same on device arrays, ordered on `stream` (a cudaStream_t; 0 is the
+ * default stream, as everywhere in CUDA); returns without synchronising. */
 int ohpic_poisson_solve_device(ohpic_poisson *solver, const double *rho, double *phi, double *e, void *stream);
 int ohpic_poisson_last_error(const ohpic_poisson *solver, char *buf, size_t len);
 

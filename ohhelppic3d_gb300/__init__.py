@@ -449,9 +449,10 @@ class PoissonSolver:
         self._check(lib().ohpic_poisson_solve(self.ptr, _dp(rho), _dp(phi), _dp(e) if e is not None else None))
         return (phi, e) if with_e else phi
 
-    def solve_device(self, rho_ptr: int, phi_ptr: int, e_ptr: int | None = None, stream: int | None = None):
+    def solve_device(self, rho_ptr: int, phi_ptr: int, e_ptr: int | None = None, stream: int = 0):
+        """Device arrays, ordered on `stream` (a cudaStream_t handle; 0 = the default stream)."""
         self._check(lib().ohpic_poisson_solve_device(self.ptr, _P(rho_ptr), _P(phi_ptr),
-                                                     _P(e_ptr) if e_ptr else None, _P(stream) if stream else None))
+                                                     _P(e_ptr) if e_ptr else None, _P(stream)))
 
     def close(self):
         if getattr(self, "ptr", None):

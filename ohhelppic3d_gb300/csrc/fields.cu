@@ -353,6 +353,18 @@ __global__ void k_wsum_to_rho(const unsigned long long *w, int64_t ncell, Specie
         rho[t] = node_rho(w + t, ncell, sc.nspecies, sc.q, r);
 }
 
+// FP64 form: rho = (sum_s q_s W_s) 2^-48 from the species' 2^-48 fixed-point
+// weight sums, the species added in a fixed order, so rho is bit-reproducible.
+__global__ void k_wsum_to_rho64(const unsigned long long *w, int64_t ncell, SpeciesCharges sc, double *rho)
+{
+    constexpr double kUnit48 = 1.0 / 281474976710656.0;   // 2^-48
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ncell; t += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int s = 0; s < sc.nspecies; ++s) acc += sc.q[s] * (double)w[s * ncell + t];
+        rho[t] = acc * kUnit48;
+    }
+}
+
 int blocks_for(int64_t n)
 {
     int64_t b = (n + 255) / 256;
@@ -362,14 +374,17 @@ int blocks_for(int64_t n)
 
 }  // namespace
 
-// FP32 form: materialise rho from the weight sums left by the last deposit.
+// Materialise rho from the fixed-point weight sums left by the last deposit.
 void ensure_rho(ohpic_ctx *c)
 {
-    if (c->cfg.precision != OHPIC_FP32 || !c->rho_from_wsum) return;
+    if (!c->rho_from_wsum) return;
     SpeciesCharges sc;
     sc.nspecies = c->cfg.nspecies;
     for (int s = 0; s < OHPIC_MAX_SPECIES; ++s) sc.q[s] = s < sc.nspecies ? c->cfg.q[s] : 0.0;
-    k_wsum_to_rho<<<blocks_for(c->g.ncell), 256, 0, c->stream>>>(c->wsum, c->g.ncell, sc, (float *)c->rho);
+    if (c->cfg.precision == OHPIC_FP32)
+        k_wsum_to_rho<<<blocks_for(c->g.ncell), 256, 0, c->stream>>>(c->wsum, c->g.ncell, sc, (float *)c->rho);
+    else
+        k_wsum_to_rho64<<<blocks_for(c->g.ncell), 256, 0, c->stream>>>(c->wsum, c->g.ncell, sc, (double *)c->rho);
     ++c->launches;
     c->rho_from_wsum = false;
 }

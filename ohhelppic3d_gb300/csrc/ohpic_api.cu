@@ -162,16 +162,13 @@ int check_upload(ohpic_ctx *c, int s)
     return rc;
 }
 
-// Clears the deposit target: rho (FP64 form) or the per-species fixed-point
-// weight sums (FP32 form, turned into rho by the next solve or download).
+// Clears the deposit target: the per-species fixed-point weight sums (units of
+// 2^-24 in the FP32 form, 2^-48 in the FP64 form), turned into rho by the next
+// solve or download.
 void zero_deposit(ohpic_ctx *c)
 {
-    if (c->cfg.precision == OHPIC_FP64) {
-        launch_zero(c, c->rho, (int64_t)c->g.ncell * 8);
-    } else {
-        launch_zero(c, c->wsum, (int64_t)c->cfg.nspecies * c->g.ncell * 8);
-        c->rho_from_wsum = true;
-    }
+    launch_zero(c, c->wsum, (int64_t)c->cfg.nspecies * c->g.ncell * 8);
+    c->rho_from_wsum = true;
 }
 
 int do_scatter(ohpic_ctx *c)
@@ -424,7 +421,7 @@ int ohpic_create(const ohpic_config *cfg, ohpic_ctx **out)
         }
     }
     if (rc == OHPIC_OK) rc = dalloc(c, (char **)&c->rho, g.ncell * es);
-    if (rc == OHPIC_OK && !f64) rc = dalloc(c, &c->wsum, (int64_t)k.nspecies * g.ncell);
+    if (rc == OHPIC_OK) rc = dalloc(c, &c->wsum, (int64_t)k.nspecies * g.ncell);
     if (rc == OHPIC_OK) rc = dalloc(c, (char **)&c->phi, g.ncell * es);
     if (rc == OHPIC_OK) rc = dalloc(c, (char **)&c->epad, (int64_t)g.gx * g.gy * g.gz * 4 * es);
     if (rc == OHPIC_OK) rc = dalloc(c, (char **)&c->spec, g.nspec * 2 * es);

@@ -122,7 +122,7 @@ struct TileArgs {
     const int64_t *tile_begin;         // [nspecies][ntile+1], absolute array indices
     const void *epad;                  // padded E
     void *rho;                         // n^3 (zeroed by the caller for deposit modes); FP64 form
-    unsigned long long *wsum;          // FP32 form: [species][n^3] sums of CIC weights, 2^-24 fixed point
+    unsigned long long *wsum;          // [species][n^3] sums of CIC weights, 2^-24 (FP32) or 2^-48 (FP64) fixed point
     double *interp_out;                // MODE_INTERP: 3 per particle slot (absolute index)
     DevDiag *diag;
     int chunk;                         // particles per CTA when unsorted
@@ -222,9 +222,9 @@ struct ohpic_ctx {
 
     // fields
     void *rho, *phi, *epad;
-    // FP32 form: the deposit accumulates per-species weight sums in 2^-24 fixed
-    // point (integer adds, so the result does not depend on the order of the
-    // atomics); the solve turns them into rho.
+    // The deposit accumulates per-species weight sums in fixed point (2^-24 in
+    // the FP32 form, 2^-48 in the FP64 form; integer adds, so the result does not
+    // depend on the order of the atomics); the solve turns them into rho.
     unsigned long long *wsum;
     bool rho_from_wsum;
     // TMA description of epad for staging a tile's E box (tma_map.cu).

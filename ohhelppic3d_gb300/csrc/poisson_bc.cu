@@ -562,7 +562,7 @@ int ohpic_poisson_solve_device(ohpic_poisson *p, const double *rho, double *phi,
 {
     if (!p || !rho || !phi) return pfail(p, OHPIC_ERR_INVALID, "poisson: null rho or phi");
     cudaSetDevice(p->dev);
-    cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+    cudaStream_t st = (cudaStream_t)stream;
     const Block &b = p->blk;
     const int64_t nl = (int64_t)b.L[0] * b.L[1] * b.L[2];
     k_pack<<<grid_of(nl), 256, 0, st>>>(b, rho, p->W);

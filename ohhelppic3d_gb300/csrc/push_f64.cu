@@ -17,15 +17,100 @@
 // drifted since the last sort, or wrapped across the periodic edge) gathers
 // from and deposits to global memory instead.
 //
-// Deposit.  A thread's consecutive particles are consecutive in cell order, so
-// their CIC weights are summed in registers while they stay in one cell and the
-// sum is added to the shared box with 8 shared atomics when the cell changes.
-// Lanes of one warp that hit the same node serialise in the shared-memory unit
-// only, which costs less than any warp-level reduction of 8 values.
+// Deposit in fixed point.  Each particle's 8 CIC weights are integers in units
+// of 2^-48 that sum to exactly 2^48: the fractional offsets are rounded to 48
+// bits, and 2^48 is split axis by axis (x, then y within each half, then z
+// within each quarter), each child rounded from the product of its parent and
+// the axis weight and its sibling taking the difference.  The products are
+// 48 x 48 -> 96-bit integer multiplies, so the weights cost no FP64 operations
+// beyond the offsets; on GB300 the FP64 pipe is the bottleneck of this form.  A
+// thread's consecutive particles are consecutive in cell order, so their
+// weights are summed in registers while they stay in one cell and added to a
+// 64-bit shared box when the cell changes; the box is flushed into per-species
+// 64-bit global sums, from which the solve forms rho = sum_s q_s W_s 2^-48 in a
+// fixed species order.  Integer addition is associative, so rho does not depend
+// on the order in which atomics land: the FP64 form is bit-reproducible.  A
+// node's sum stays below 2^64 up to 65536 particle weights per species; a flush
+// that would wrap raises OHPIC_ERR_CAPACITY.
 #include "tile_common.cuh"
 
 namespace ohpic {
 namespace {
+
+constexpr unsigned long long kOne48 = 1ull << 48;
+
+// round(r * 2^48) for r in [0, 1]: r + 16 has its last mantissa bit at 2^-48.
+__device__ __forceinline__ unsigned long long frac48(double r)
+{
+    return (unsigned long long)__double_as_longlong(r + 16.0) & ((1ull << 52) - 1);
+}
+
+// round(p * w / 2^48) for p, w <= 2^48, from the 96-bit product.
+__device__ __forceinline__ unsigned long long mul48(unsigned long long p, unsigned long long w)
+{
+    const unsigned long long hi = __umul64hi(p, w), lo = p * w;
+    const unsigned long long q = (hi << 16) | (lo >> 48);
+    return q + ((lo >> 47) & 1ull);
+}
+
+// The 8 weights of a particle with offsets rx, ry, rz in [0, 1), in units of
+// 2^-48, summing to exactly 2^48; order x fastest as in add8 / deposit_global.
+__device__ __forceinline__ void fixed_weights48(int conv, double rx, double ry, double rz, unsigned long long u[8])
+{
+    const unsigned long long Rx = frac48(rx), Ry = frac48(ry), Rz = frac48(rz);
+    const bool ref = conv == OHPIC_WEIGHTS_REFERENCE;   // node floor(x) takes r (linear_scatter.f90:41-42)
+    const unsigned long long X1 = ref ? kOne48 - Rx : Rx, X0 = kOne48 - X1;
+    const unsigned long long wy1 = ref ? kOne48 - Ry : Ry, wz1 = ref ? kOne48 - Rz : Rz;
+    const unsigned long long Y01 = min(mul48(X0, wy1), X0), Y11 = min(mul48(X1, wy1), X1);
+    const unsigned long long Y00 = X0 - Y01, Y10 = X1 - Y11;
+    const unsigned long long Z00 = min(mul48(Y00, wz1), Y00), Z10 = min(mul48(Y10, wz1), Y10);
+    const unsigned long long Z01 = min(mul48(Y01, wz1), Y01), Z11 = min(mul48(Y11, wz1), Y11);
+    u[0] = Y00 - Z00; u[1] = Y10 - Z10; u[2] = Y01 - Z01; u[3] = Y11 - Z11;
+    u[4] = Z00; u[5] = Z10; u[6] = Z01; u[7] = Z11;
+}
+
+__device__ __forceinline__ void add_checked(unsigned long long *p, unsigned long long v, DevDiag *d)
+{
+    const unsigned long long old = atomicAdd(p, v);
+    if (old + v < old) flag_error(d, OHPIC_ERR_CAPACITY, 20);
+}
+
+// The 8 weights of a particle outside the staged box, straight into the global sums.
+__device__ __forceinline__ void deposit_global48(const Geom &g, unsigned long long *w, int ix, int iy, int iz,
+                                                 const unsigned long long u[8], DevDiag *d)
+{
+    const int ix1 = ix + 1 == g.nx ? 0 : ix + 1;
+    const int iy1 = iy + 1 == g.ny ? 0 : iy + 1;
+    const int iz1 = iz + 1 == g.nz ? 0 : iz + 1;
+    const int64_t y0 = (int64_t)iy * g.nx, y1 = (int64_t)iy1 * g.nx;
+    const int64_t z0 = (int64_t)iz * g.nx * g.ny, z1 = (int64_t)iz1 * g.nx * g.ny;
+    add_checked(w + ix + y0 + z0, u[0], d);
+    add_checked(w + ix1 + y0 + z0, u[1], d);
+    add_checked(w + ix + y1 + z0, u[2], d);
+    add_checked(w + ix1 + y1 + z0, u[3], d);
+    add_checked(w + ix + y0 + z1, u[4], d);
+    add_checked(w + ix1 + y0 + z1, u[5], d);
+    add_checked(w + ix + y1 + z1, u[6], d);
+    add_checked(w + ix1 + y1 + z1, u[7], d);
+}
+
+// The shared box into the species' global sums, one atomic per non-zero node.
+__device__ __forceinline__ void flush_box48(const TileArgs &a, const Item &it, const unsigned long long *box)
+{
+    const Geom &g = a.g;
+    unsigned long long *w = a.wsum + (int64_t)it.sp * g.ncell;
+    const int s3 = g.sx * g.sy * g.sz;
+    for (int i = threadIdx.x; i < s3; i += blockDim.x) {
+        const unsigned long long v = box[i];
+        if (v) {
+            const int ax = i % g.sx, by = (i / g.sx) % g.sy, cz = i / (g.sx * g.sy);
+            const int x = wrapi(it.x0 - g.halo + ax, g.nx);
+            const int y = wrapi(it.y0 - g.halo + by, g.ny);
+            const int z = wrapi(it.z0 - g.halo + cz, g.nz);
+            add_checked(w + x + (int64_t)g.nx * (y + (int64_t)g.ny * z), v, a.diag);
+        }
+    }
+}
 
 // ===========================================================================
 // FP64 form: 2 particles per thread (double2 loads/stores).
@@ -46,9 +131,9 @@ __global__ void __launch_bounds__(256, 2) tiled_f64(TileArgs a, PartF64 p)
     extern __shared__ __align__(32) unsigned char smem[];
     const int s3 = g.sx * g.sy * g.sz;
     dnode *sE = (dnode *)smem;
-    double *srho = (double *)(smem + (kGather ? (size_t)s3 * sizeof(dnode) : 0));
+    unsigned long long *sbox = (unsigned long long *)(smem + (kGather ? (size_t)s3 * sizeof(dnode) : 0));
     if (box.on) {
-        stage_tile<dnode, double>(a, it, sE, srho, kGather, kDeposit);
+        stage_tile<dnode, unsigned long long>(a, it, sE, sbox, kGather, kDeposit);
         __syncthreads();
     }
 
@@ -59,7 +144,8 @@ __global__ void __launch_bounds__(256, 2) tiled_f64(TileArgs a, PartF64 p)
     const long long bnx = __double_as_longlong(fnx), bny = __double_as_longlong(fny), bnz = __double_as_longlong(fnz);
     unsigned ncx = 0, ncy = 0, ncz = 0, nout = 0;
     double ke = 0.0, px = 0.0, py = 0.0, pz = 0.0;
-    Run<double> run;
+    Run<unsigned long long> run;
+    unsigned long long *wsum = a.wsum + (int64_t)sp * g.ncell;
 
     for (int64_t grp = it.g0 + threadIdx.x; grp < it.g1; grp += blockDim.x) {
         const int64_t i0 = grp * PPT;
@@ -177,20 +263,15 @@ __global__ void __launch_bounds__(256, 2) tiled_f64(TileArgs a, PartF64 p)
                     flag_error(a.diag, OHPIC_ERR_BOUNDS, 2);
                     continue;
                 }
-                double wx0, wx1, wy0, wy1, wz0, wz1;
-                cic<double>(a.weights, x - (double)jx, wx0, wx1);
-                cic<double>(a.weights, y - (double)jy, wy0, wy1);
-                cic<double>(a.weights, z - (double)jz, wz0, wz1);
-                // amount*rx*ry*rz (linear_scatter.f90:47-49), factored without changing rounding.
-                const double q0 = c.q * wx0, q1 = c.q * wx1;
-                const double b00 = q0 * wy0, b10 = q1 * wy0, b01 = q0 * wy1, b11 = q1 * wy1;
-                const double w[8] = {b00 * wz0, b10 * wz0, b01 * wz0, b11 * wz0,
-                                     b00 * wz1, b10 * wz1, b01 * wz1, b11 * wz1};
+                // rx*ry*rz of linear_scatter.f90:41-52 in 2^-48 fixed point; the
+                // charge amount is applied per species when rho is formed
+                unsigned long long w[8];
+                fixed_weights48(a.weights, x - (double)jx, y - (double)jy, z - (double)jz, w);
                 const int key = box.key(jx, jy, jz);
                 if (key >= 0) {
-                    run.add(key, w, srho, box.sx, box.sxy);
+                    run.add(key, w, sbox, box.sx, box.sxy);
                 } else {
-                    deposit_global<double>(g, (double *)a.rho, jx, jy, jz, w);
+                    deposit_global48(g, wsum, jx, jy, jz, w, a.diag);
                     if (!kGather) ++nout;
                 }
             }
@@ -204,10 +285,10 @@ __global__ void __launch_bounds__(256, 2) tiled_f64(TileArgs a, PartF64 p)
             *(double2 *)(p.vz + i0) = make_double2(VZ[0], VZ[1]);
         }
     }
-    if (kDeposit) run.flush(srho, box.sx, box.sxy);
+    if (kDeposit) run.flush(sbox, box.sx, box.sxy);
     if (kDeposit && box.on) {
         __syncthreads();
-        flush_tile<double>(a, it, srho);
+        flush_box48(a, it, sbox);
     }
     if (kMove || kGather) flush_diag<double>(a, sp, ncx, ncy, ncz, nout, ke, px, py, pz);
 }

@@ -73,6 +73,7 @@ __device__ __forceinline__ int wrapi(int i, int n)
 
 __device__ __forceinline__ void atomic_add_t(float *p, float v) { atomicAdd(p, v); }
 __device__ __forceinline__ void atomic_add_t(double *p, double v) { atomicAdd(p, v); }
+__device__ __forceinline__ void atomic_add_t(unsigned long long *p, unsigned long long v) { atomicAdd(p, v); }
 
 // 8 corner contributions of one cell into a box with row pitch sx and plane pitch sxy.
 template <typename T>

@@ -84,12 +84,13 @@ def test_device_entry_point_on_caller_stream(ohpic, oracle_mod):
     phi_o, e_o = O.poisson_bc(rho, kinds, corrected=True)
     dev = torch.device("cuda", 0)
     r = torch.tensor(rho, device=dev)
-    phi = torch.empty_like(r)
-    e = torch.empty((3,) + tuple(r.shape), dtype=torch.float64, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    phi = torch.full_like(r, float("nan"))
+    e = torch.full((3,) + tuple(r.shape), float("nan"), dtype=torch.float64, device=dev)
+    side = torch.cuda.Stream(dev)                 # a non-default stream: the solve must follow it
+    side.wait_stream(torch.cuda.current_stream(dev))
     with P.PoissonSolver(n, kinds, table=P.TABLE_CORRECTED) as s:
         for _ in range(2):
-            s.solve_device(r.data_ptr(), phi.data_ptr(), e.data_ptr(), stream.cuda_stream)
-        stream.synchronize()
+            s.solve_device(r.data_ptr(), phi.data_ptr(), e.data_ptr(), side.cuda_stream)
+        side.synchronize()
     assert np.max(np.abs(phi.cpu().numpy() - phi_o)) <= 1e-11 * np.max(np.abs(phi_o))
     assert np.max(np.abs(e.cpu().numpy() - e_o)) <= 1e-11 * np.max(np.abs(e_o))

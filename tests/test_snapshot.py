@@ -1,9 +1,9 @@
 """Checkpoint and restart through ohpic_snapshot_save / ohpic_snapshot_load.
 
 A run interrupted after 7 steps and restarted from its snapshot in a fresh
-context must continue like the uninterrupted run: bit for bit in the FP32 form
-(its deposit is integer fixed point, so re-depositing the restored particles
-gives the same sums), within FP64 atomic rounding in the FP64 form.  Snapshots
+context must continue like the uninterrupted run, bit for bit in both forms
+(their deposits are integer fixed point, so re-depositing the restored
+particles gives the same sums whatever order the atomics land in).  Snapshots
 of another grid, truncated or foreign bytes, and cells outside the grid are
 refused with a status code.
 """
@@ -50,18 +50,11 @@ def test_restart_continues_the_run(ohpic, precision):
         d = b.diagnostics()
     assert d["step"] == ref_d["step"] == 13
     assert d["count"] == ref_d["count"]
-    if precision == "fp32":
-        assert np.array_equal(rho, ref_rho)
-        for s in range(2):
-            for k in KEYS:
-                assert np.array_equal(got[s][k], ref[s][k]), (s, k)
-        assert d["crossings"] == ref_d["crossings"]
-    else:
-        # FP64 atomics add in a different order in the two runs
-        assert np.max(np.abs(rho - ref_rho)) <= 1e-9 * np.max(np.abs(ref_rho))
-        for s in range(2):
-            for k in KEYS:
-                assert np.max(np.abs(got[s][k] - ref[s][k])) <= 1e-9 * max(1.0, np.max(np.abs(ref[s][k]))), (s, k)
+    assert np.array_equal(rho, ref_rho)
+    for s in range(2):
+        for k in KEYS:
+            assert np.array_equal(got[s][k], ref[s][k]), (s, k)
+    assert d["crossings"] == ref_d["crossings"]
 
 
 def test_snapshot_mismatch_is_refused(ohpic):

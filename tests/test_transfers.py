@@ -66,8 +66,4 @@ def test_pinned_and_pageable_transfers_agree(ohpic, precision):
         a.step(0.1, 2)
         b.step(0.1, 2)
         fa, fb = a.field(P.RHO), b.field(P.RHO)
-        if precision == "fp32":
-            assert np.array_equal(fa, fb)          # integer fixed-point deposit
-        else:
-            # FP64 atomics land in a different order from run to run
-            assert np.max(np.abs(fa - fb)) <= 1e-12 * np.max(np.abs(fa))
+        assert np.array_equal(fa, fb)              # integer fixed-point deposit in both forms
