@@ -155,6 +155,36 @@ private:
     Context &c_;
 };
 
+// t_PoissonFieldSolver with a boundary kind per axis (poisson_field_solver.f90:34-175,
+// poisson_solver3d.f90:28-207) on the global block 0..n: rho and phi hold
+// (n[0]+1)(n[1]+1)(n[2]+1) nodes, x fastest; e three such blocks (or empty).
+class BoundedFieldSolver {
+public:
+    BoundedFieldSolver(const int32_t n[3], const int32_t kinds[3], const double boundary_values[6],
+                       int32_t table = OHPIC_TABLE_AS_WRITTEN, int32_t device = 0)
+    {
+        const int rc = ohpic_poisson_create(n, kinds, boundary_values, table, device, &s_);
+        if (rc != OHPIC_OK) throw Error(rc, std::string("ohpic_poisson_create: ") + ohpic_status_string(rc));
+    }
+    ~BoundedFieldSolver()
+    {
+        if (s_) ohpic_poisson_destroy(s_);
+    }
+    BoundedFieldSolver(const BoundedFieldSolver &) = delete;
+    BoundedFieldSolver &operator=(const BoundedFieldSolver &) = delete;
+    void solve(const double *rho, double *phi, double *e = nullptr)
+    {
+        const int rc = ohpic_poisson_solve(s_, rho, phi, e);
+        if (rc == OHPIC_OK) return;
+        char buf[512] = {0};
+        ohpic_poisson_last_error(s_, buf, sizeof(buf));
+        throw Error(rc, std::string("poisson_solve: ") + ohpic_status_string(rc) + " (" + buf + ")");
+    }
+
+private:
+    ohpic_poisson *s_ = nullptr;
+};
+
 // particle_mover_factory.f90:25-30: "boris" is the only mover.
 inline ParticleMover create_particle_mover(const std::string &name, Context &c)
 {

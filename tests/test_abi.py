@@ -110,8 +110,15 @@ int main(int argc, char **argv)
         try { double p[6] = {0}; double eb[6] = {0}; ohpic::create_particle_mover("boris", c).move(p, -1.0, eb, 0.1); }
         catch (const ohpic::Error &x) { unsupported = x.status(); }
         try { ohpic::create_particle_mover("leapfrog", c); } catch (const ohpic::Error &x) { unknown = x.status(); }
-        std::printf("ok %lld %lld %zu %d %d %.17g\n", (long long)d.count[0], (long long)d.count[1], e.size(),
-                    unsupported, unknown, d.total_charge);
+        // a unit charge at the centre of a 4^3 block with walls on x, mirrors on y, periodic z
+        const int32_t nb[3] = {4, 4, 4}, kinds[3] = {OHPIC_BC_DIRICHLET, OHPIC_BC_NEUMANN, OHPIC_BC_PERIODIC};
+        const double bv[6] = {0, 0, 0, 0, 0, 0};
+        ohpic::BoundedFieldSolver bs(nb, kinds, bv, OHPIC_TABLE_CORRECTED);
+        std::vector<double> rho(125, 0.0), phi(125, 0.0);
+        rho[2 + 5 * (2 + 5 * 2)] = 1.0;
+        bs.solve(rho.data(), phi.data());
+        std::printf("ok %lld %lld %zu %d %d %.17g %.17g %.17g\n", (long long)d.count[0], (long long)d.count[1],
+                    e.size(), unsupported, unknown, d.total_charge, phi[2 + 5 * (2 + 5 * 2)], phi[0]);
     } catch (const ohpic::Error &x) {
         std::printf("error %d %s\n", x.status(), x.what());
     }
@@ -158,3 +165,5 @@ def test_cpp_mirror_runs_the_path(ohpic, tmp_path):
     assert unsupported == ohpic.ERR_UNSUPPORTED and unknown == ohpic.ERR_INVALID
     # FP32 rho: neutral to rounding, relative to the 4 * 512 * 0.125 = 256 charge per species
     assert abs(float(words[6])) < 1e-9 * 256 * 100
+    # the bounded solve: a positive potential at the charge, zero on the Dirichlet wall
+    assert float(words[7]) > 0.0 and float(words[8]) == 0.0
