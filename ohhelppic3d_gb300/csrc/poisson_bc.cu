@@ -22,9 +22,10 @@
 //                       FFTW's separable R2HC/HC2R for a Poisson solve).
 // The working array is complex, so every transform applies to real and
 // imaginary parts alike (they are all linear), whatever order the axes come in.
-// Lines along x are contiguous in the extension buffer; lines along y and z are
-// interleaved (one transform per line, stride = line count), so both the
-// gathers and the scatters of the extension kernels stay coalesced.
+// Every extension is stored line-contiguous, so cuFFT runs contiguous batched
+// transforms on every axis; along y and z the extension and extraction kernels
+// transpose 32 x 32 tiles through shared memory so that both their reads and
+// their writes stay coalesced.
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <math.h>
@@ -134,11 +135,6 @@ __device__ __forceinline__ int64_t w_index(const Lines &m, int64_t line, int j)
     return line + (int64_t)m.L0 * m.L1 * j;
 }
 
-__device__ __forceinline__ int64_t b_index(const Lines &m, int64_t line, int mi)
-{
-    return m.axis == 0 ? line * m.M + mi : (int64_t)mi * m.lines + line;
-}
-
 // (a + ib) e^{-i pi num / den}
 __device__ __forceinline__ double2 rotate(double2 v, double num, double den)
 {
@@ -147,89 +143,129 @@ __device__ __forceinline__ double2 rotate(double2 v, double num, double den)
     return make_double2(v.x * c + v.y * s, v.y * c - v.x * s);
 }
 
-__global__ void k_extend(Lines m, int xf, int L, const double2 *W, double2 *B)
+// Extension element mi of line `line` for transform xf (see the header).
+__device__ __forceinline__ double2 ext_value(const Lines &m, int xf, int L, const double2 *W, int64_t line, int mi)
 {
-    const int64_t total = (int64_t)m.M * m.lines;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t line;
-        int mi;
-        if (m.axis == 0) {
-            line = t / m.M;
-            mi = (int)(t - line * m.M);
-        } else {
-            mi = (int)(t / m.lines);
-            line = t - (int64_t)mi * m.lines;
-        }
-        int j = -1;
-        double sgn = 1.0;
-        bool twiddle = false;
-        switch (xf) {
-        case XF_DFT:
-        case XF_IDFT: j = mi; break;
-        case XF_DCT1: j = mi < L ? mi : m.M - mi; break;
-        case XF_DST1:
-            if (mi == 0 || mi == L + 1) j = -1;
-            else if (mi <= L) j = mi - 1;
-            else { j = m.M - mi - 1; sgn = -1.0; }
-            break;
-        case XF_DCT2: j = mi < L ? mi : 2 * L - 1 - mi; break;
-        case XF_DST2:
-            j = mi < L ? mi : 2 * L - 1 - mi;
-            sgn = (j & 1) ? -1.0 : 1.0;
-            break;
-        default:   // DCT3, DST3 (the latter on the reversed line)
-            if (mi == L) j = -1;
-            else if (mi < L) j = mi;
-            else { j = 2 * L - mi; sgn = -1.0; }
-            if (xf == XF_DST3 && j >= 0) j = L - 1 - j;
-            twiddle = true;
-            break;
-        }
-        double2 v = make_double2(0.0, 0.0);
-        if (j >= 0) {
-            v = W[w_index(m, line, j)];
-            v.x *= sgn;
-            v.y *= sgn;
-        }
-        if (twiddle) v = rotate(v, (double)mi, 2.0 * L);
-        B[b_index(m, line, mi)] = v;
+    int j = -1;
+    double sgn = 1.0;
+    bool twiddle = false;
+    switch (xf) {
+    case XF_DFT:
+    case XF_IDFT: j = mi; break;
+    case XF_DCT1: j = mi < L ? mi : m.M - mi; break;
+    case XF_DST1:
+        if (mi == 0 || mi == L + 1) j = -1;
+        else if (mi <= L) j = mi - 1;
+        else { j = m.M - mi - 1; sgn = -1.0; }
+        break;
+    case XF_DCT2: j = mi < L ? mi : 2 * L - 1 - mi; break;
+    case XF_DST2:
+        j = mi < L ? mi : 2 * L - 1 - mi;
+        sgn = (j & 1) ? -1.0 : 1.0;
+        break;
+    default:   // DCT3, DST3 (the latter on the reversed line)
+        if (mi == L) j = -1;
+        else if (mi < L) j = mi;
+        else { j = 2 * L - mi; sgn = -1.0; }
+        if (xf == XF_DST3 && j >= 0) j = L - 1 - j;
+        twiddle = true;
+        break;
+    }
+    double2 v = make_double2(0.0, 0.0);
+    if (j >= 0) {
+        v = W[w_index(m, line, j)];
+        v.x *= sgn;
+        v.y *= sgn;
+    }
+    if (twiddle) v = rotate(v, (double)mi, 2.0 * L);
+    return v;
+}
+
+// Output element k of line `line` from its transformed extension Z (= B + line * M).
+__device__ __forceinline__ double2 extract_value(int xf, int L, const double2 *Z, int k)
+{
+    switch (xf) {
+    case XF_DST1: {
+        const double2 z = Z[k + 1];
+        return make_double2(-z.y, z.x);
+    }
+    case XF_DCT2: return rotate(Z[k], (double)k, 2.0 * L);
+    case XF_DST2: {
+        const int kk = L - 1 - k;
+        return rotate(Z[kk], (double)kk, 2.0 * L);
+    }
+    case XF_DST3: {
+        const double2 z = Z[k];
+        return (k & 1) ? make_double2(-z.x, -z.y) : z;
+    }
+    default: return Z[k];   // DFT, IDFT, DCT1, DCT3
     }
 }
 
-__global__ void k_extract(Lines m, int xf, int L, const double2 *B, double2 *W)
+// Every extension is stored line-contiguous, B[line * M + mi], so one batched
+// cuFFT plan of contiguous transforms serves every axis.  Along x the lines of W
+// are contiguous too and a thread per (line, mi) reads and writes coalesced.
+// Along y and z consecutive lines are consecutive in W instead, so 32 x 32
+// tiles go through shared memory: reads run along lines, writes along mi.
+constexpr int kTile = 32, kTileRows = 8;
+
+__global__ void k_extend_x(Lines m, int xf, int L, const double2 *W, double2 *B)
+{
+    const int64_t total = (int64_t)m.M * m.lines;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t line = t / m.M;
+        const int mi = (int)(t - line * m.M);
+        B[t] = ext_value(m, xf, L, W, line, mi);
+    }
+}
+
+__global__ void k_extract_x(Lines m, int xf, int L, const double2 *B, double2 *W)
 {
     const int64_t total = (int64_t)L * m.lines;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t line;
-        int k;
-        if (m.axis == 0) {
-            line = t / L;
-            k = (int)(t - line * L);
-        } else {
-            k = (int)(t / m.lines);
-            line = t - (int64_t)k * m.lines;
-        }
-        double2 y;
-        switch (xf) {
-        case XF_DST1: {
-            const double2 z = B[b_index(m, line, k + 1)];
-            y = make_double2(-z.y, z.x);
-            break;
-        }
-        case XF_DCT2: y = rotate(B[b_index(m, line, k)], (double)k, 2.0 * L); break;
-        case XF_DST2: {
-            const int kk = L - 1 - k;
-            y = rotate(B[b_index(m, line, kk)], (double)kk, 2.0 * L);
-            break;
-        }
-        case XF_DST3: {
-            const double2 z = B[b_index(m, line, k)];
-            y = (k & 1) ? make_double2(-z.x, -z.y) : z;
-            break;
-        }
-        default: y = B[b_index(m, line, k)]; break;   // DFT, IDFT, DCT1, DCT3
-        }
-        W[w_index(m, line, k)] = y;
+        const int64_t line = t / L;
+        const int k = (int)(t - line * L);
+        W[w_index(m, line, k)] = extract_value(xf, L, B + line * m.M, k);
+    }
+}
+
+// grid (ceil(lines / 32), ceil(M / 32)), block (32, 8)
+__global__ void k_extend_yz(Lines m, int xf, int L, const double2 *W, double2 *B)
+{
+    __shared__ double2 tile[kTile][kTile + 1];
+    const int64_t l0 = (int64_t)blockIdx.x * kTile;
+    const int m0 = blockIdx.y * kTile;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    for (int r = ty; r < kTile; r += kTileRows) {
+        const int64_t line = l0 + tx;
+        const int mi = m0 + r;
+        if (line < m.lines && mi < m.M) tile[r][tx] = ext_value(m, xf, L, W, line, mi);
+    }
+    __syncthreads();
+    for (int r = ty; r < kTile; r += kTileRows) {
+        const int64_t line = l0 + r;
+        const int mi = m0 + tx;
+        if (line < m.lines && mi < m.M) B[line * m.M + mi] = tile[tx][r];
+    }
+}
+
+// grid (ceil(lines / 32), ceil(L / 32)), block (32, 8)
+__global__ void k_extract_yz(Lines m, int xf, int L, const double2 *B, double2 *W)
+{
+    __shared__ double2 tile[kTile][kTile + 1];
+    const int64_t l0 = (int64_t)blockIdx.x * kTile;
+    const int k0 = blockIdx.y * kTile;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    for (int r = ty; r < kTile; r += kTileRows) {
+        const int64_t line = l0 + r;
+        const int k = k0 + tx;
+        if (line < m.lines && k < L) tile[r][tx] = extract_value(xf, L, B + line * m.M, k);
+    }
+    __syncthreads();
+    for (int r = ty; r < kTile; r += kTileRows) {
+        const int64_t line = l0 + tx;
+        const int k = k0 + r;
+        if (line < m.lines && k < L) W[w_index(m, line, k)] = tile[tx][r];
     }
 }
 
@@ -407,13 +443,22 @@ int transform(ohpic_poisson *p, int d, int xf, cudaStream_t st)
 {
     const Lines &m = p->lines[d];
     const int L = p->ax[d].L;
-    k_extend<<<grid_of((int64_t)m.M * m.lines), 256, 0, st>>>(m, xf, L, p->W, p->B);
+    const unsigned lt = (unsigned)((m.lines + kTile - 1) / kTile);
+    if (d == 0)
+        k_extend_x<<<grid_of((int64_t)m.M * m.lines), 256, 0, st>>>(m, xf, L, p->W, p->B);
+    else
+        k_extend_yz<<<dim3(lt, (unsigned)((m.M + kTile - 1) / kTile)), dim3(kTile, kTileRows), 0, st>>>(m, xf, L, p->W,
+                                                                                                      p->B);
     if (cufftSetStream(p->plan[d], st) != CUFFT_SUCCESS)
         return pfail(p, OHPIC_ERR_CUDA, "cufftSetStream failed");
     const int dir = xf == XF_IDFT ? CUFFT_INVERSE : CUFFT_FORWARD;
     const cufftResult r = cufftExecZ2Z(p->plan[d], (cufftDoubleComplex *)p->B, (cufftDoubleComplex *)p->B, dir);
     if (r != CUFFT_SUCCESS) return pfail(p, OHPIC_ERR_CUDA, "cufftExecZ2Z failed (" + std::to_string((int)r) + ")");
-    k_extract<<<grid_of((int64_t)L * m.lines), 256, 0, st>>>(m, xf, L, p->B, p->W);
+    if (d == 0)
+        k_extract_x<<<grid_of((int64_t)L * m.lines), 256, 0, st>>>(m, xf, L, p->B, p->W);
+    else
+        k_extract_yz<<<dim3(lt, (unsigned)((L + kTile - 1) / kTile)), dim3(kTile, kTileRows), 0, st>>>(m, xf, L, p->B,
+                                                                                                     p->W);
     return OHPIC_OK;
 }
 
@@ -529,12 +574,7 @@ int ohpic_poisson_create(const int32_t n[3], const int32_t kinds[3], const doubl
         }
         const Lines &m = p->lines[d];
         int len = m.M, emb = m.M;
-        cufftResult r;
-        if (d == 0)
-            r = cufftPlanMany(&p->plan[d], 1, &len, &emb, 1, m.M, &emb, 1, m.M, CUFFT_Z2Z, (int)m.lines);
-        else
-            r = cufftPlanMany(&p->plan[d], 1, &len, &emb, (int)m.lines, 1, &emb, (int)m.lines, 1, CUFFT_Z2Z,
-                              (int)m.lines);
+        const cufftResult r = cufftPlanMany(&p->plan[d], 1, &len, &emb, 1, m.M, &emb, 1, m.M, CUFFT_Z2Z, (int)m.lines);
         if (r != CUFFT_SUCCESS) {
             rc = pfail(p, OHPIC_ERR_CUDA, "cufftPlanMany failed (" + std::to_string((int)r) + ")");
             break;
