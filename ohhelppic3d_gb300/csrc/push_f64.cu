@@ -11,8 +11,8 @@
 // cell index (sort.cu), so the particles of one tile are one contiguous range.
 // One CTA takes (species, tile, part): it stages the tile's node E field plus a
 // halo of `halo` cells into shared memory, zeroes a shared rho box of the same
-// extent, streams its particles with 16-byte vector loads and stores (2 FP64
-// or 4 FP32 particles per thread per iteration) and flushes the rho box to
+// extent, streams its particles with loads and stores coalesced across the
+// warp (one FP64 particle per thread per iteration) and flushes the box to
 // global memory once.  A particle whose cell lies outside the staged box (it
 // drifted since the last sort, or wrapped across the periodic edge) gathers
 // from and deposits to global memory instead.
@@ -38,6 +38,7 @@ namespace ohpic {
 namespace {
 
 constexpr unsigned long long kOne48 = 1ull << 48;
+constexpr int kF64PerThread = 1;
 
 // round(r * 2^48) for r in [0, 1]: r + 16 has its last mantissa bit at 2^-48.
 __device__ __forceinline__ unsigned long long frac48(double r)
@@ -113,12 +114,83 @@ __device__ __forceinline__ void flush_box48(const TileArgs &a, const Item &it, c
 }
 
 // ===========================================================================
-// FP64 form: 2 particles per thread (double2 loads/stores).
+// FP64 form: kF64PerThread consecutive particles per thread per iteration.  One
+// (scalar loads, still coalesced across the warp) keeps the per-thread state
+// within the two-CTA register budget without spills; two (double2 vectors)
+// spilled 124 bytes per thread even with three-component node loads.
 // ===========================================================================
+// The three E components of a node (the padded node's fourth is never read).
+struct d3 {
+    double x, y, z;
+};
+
+__device__ __forceinline__ d3 node3(const dnode *p, bool shared)
+{
+    d3 r;
+    if (shared) {
+        const double2 a = *(const double2 *)p;
+        r.x = a.x;
+        r.y = a.y;
+        r.z = p->z;
+    } else {
+        const double2 a = __ldg((const double2 *)p);
+        r.x = a.x;
+        r.y = a.y;
+        r.z = __ldg(&p->z);
+    }
+    return r;
+}
+
+// E nodes of the cell with low corner (ix, iy, iz): from the staged box when key >= 0.
+__device__ __forceinline__ void load_nodes3(const TileArgs &a, const Box &b, int key, int ix, int iy, int iz,
+                                            const dnode *sE, d3 nd[8])
+{
+    const dnode *q;
+    int64_t sx, sxy;
+    const bool in = key >= 0;
+    if (in) {
+        q = sE + key;
+        sx = b.sx;
+        sxy = b.sxy;
+    } else {
+        const Geom &g = a.g;
+        sx = g.gx;
+        sxy = (int64_t)g.gx * g.gy;
+        q = (const dnode *)a.epad + (ix + g.halo) + sx * (iy + g.halo) + sxy * (iz + g.halo);
+    }
+    nd[0] = node3(q, in);
+    nd[1] = node3(q + 1, in);
+    nd[2] = node3(q + sx, in);
+    nd[3] = node3(q + sx + 1, in);
+    nd[4] = node3(q + sxy, in);
+    nd[5] = node3(q + sxy + 1, in);
+    nd[6] = node3(q + sxy + sx, in);
+    nd[7] = node3(q + sxy + sx + 1, in);
+}
+
+template <int PPT>
+__device__ __forceinline__ void load_f64(const double *a, int64_t i0, double v[PPT])
+{
+    if constexpr (PPT == 2) {
+        const double2 t = *(const double2 *)(a + i0);
+        v[0] = t.x;
+        v[1] = t.y;
+    } else {
+        v[0] = a[i0];
+    }
+}
+
+template <int PPT>
+__device__ __forceinline__ void store_f64(double *a, int64_t i0, const double v[PPT])
+{
+    if constexpr (PPT == 2) *(double2 *)(a + i0) = make_double2(v[0], v[1]);
+    else a[i0] = v[0];
+}
+
 template <int MODE, bool STRICT>
 __global__ void __launch_bounds__(256, 2) tiled_f64(TileArgs a, PartF64 p)
 {
-    constexpr int PPT = 2;
+    constexpr int PPT = kF64PerThread;
     using Ops = typename std::conditional<STRICT, StrictOps, FastOps>::type;
     constexpr bool kGather = MODE != MODE_DEPOSIT;
     constexpr bool kMove = MODE == MODE_PUSH || MODE == MODE_MOVE;
@@ -150,16 +222,13 @@ __global__ void __launch_bounds__(256, 2) tiled_f64(TileArgs a, PartF64 p)
     for (int64_t grp = it.g0 + threadIdx.x; grp < it.g1; grp += blockDim.x) {
         const int64_t i0 = grp * PPT;
         double X[PPT], Y[PPT], Z[PPT], VX[PPT], VY[PPT], VZ[PPT];
-        {
-            double2 t;
-            t = *(const double2 *)(p.x + i0); X[0] = t.x; X[1] = t.y;
-            t = *(const double2 *)(p.y + i0); Y[0] = t.x; Y[1] = t.y;
-            t = *(const double2 *)(p.z + i0); Z[0] = t.x; Z[1] = t.y;
-            if (kGather) {
-                t = *(const double2 *)(p.vx + i0); VX[0] = t.x; VX[1] = t.y;
-                t = *(const double2 *)(p.vy + i0); VY[0] = t.x; VY[1] = t.y;
-                t = *(const double2 *)(p.vz + i0); VZ[0] = t.x; VZ[1] = t.y;
-            }
+        load_f64<PPT>(p.x, i0, X);
+        load_f64<PPT>(p.y, i0, Y);
+        load_f64<PPT>(p.z, i0, Z);
+        if (kGather) {
+            load_f64<PPT>(p.vx, i0, VX);
+            load_f64<PPT>(p.vy, i0, VY);
+            load_f64<PPT>(p.vz, i0, VZ);
         }
 #pragma unroll
         for (int j = 0; j < PPT; ++j) {
@@ -174,8 +243,8 @@ __global__ void __launch_bounds__(256, 2) tiled_f64(TileArgs a, PartF64 p)
                 }
                 const int key = box.key(ix, iy, iz);
                 nout += key < 0;
-                dnode nd[8];
-                load_nodes<dnode>(a, box, key, ix, iy, iz, sE, nd);
+                d3 nd[8];
+                load_nodes3(a, box, key, ix, iy, iz, sE, nd);
                 double wx0, wx1, wy0, wy1, wz0, wz1;
                 cic<double>(a.weights, Ops::sub(x, (double)ix), wx0, wx1);
                 cic<double>(a.weights, Ops::sub(y, (double)iy), wy0, wy1);
@@ -191,7 +260,7 @@ __global__ void __launch_bounds__(256, 2) tiled_f64(TileArgs a, PartF64 p)
                         for (int jj = 0; jj < 2; ++jj)
 #pragma unroll
                             for (int kk = 0; kk < 2; ++kk) {
-                                const dnode v = nd[ii + 2 * jj + 4 * kk];
+                                const d3 v = nd[ii + 2 * jj + 4 * kk];
                                 ex = Ops::add(ex, Ops::mul(Ops::mul(Ops::mul(v.x, wxs[ii]), wys[jj]), wzs[kk]));
                                 ey = Ops::add(ey, Ops::mul(Ops::mul(Ops::mul(v.y, wxs[ii]), wys[jj]), wzs[kk]));
                                 ez = Ops::add(ez, Ops::mul(Ops::mul(Ops::mul(v.z, wxs[ii]), wys[jj]), wzs[kk]));
@@ -277,12 +346,12 @@ __global__ void __launch_bounds__(256, 2) tiled_f64(TileArgs a, PartF64 p)
             }
         }
         if (kMove) {
-            *(double2 *)(p.x + i0) = make_double2(X[0], X[1]);
-            *(double2 *)(p.y + i0) = make_double2(Y[0], Y[1]);
-            *(double2 *)(p.z + i0) = make_double2(Z[0], Z[1]);
-            *(double2 *)(p.vx + i0) = make_double2(VX[0], VX[1]);
-            *(double2 *)(p.vy + i0) = make_double2(VY[0], VY[1]);
-            *(double2 *)(p.vz + i0) = make_double2(VZ[0], VZ[1]);
+            store_f64<PPT>(p.x, i0, X);
+            store_f64<PPT>(p.y, i0, Y);
+            store_f64<PPT>(p.z, i0, Z);
+            store_f64<PPT>(p.vx, i0, VX);
+            store_f64<PPT>(p.vy, i0, VY);
+            store_f64<PPT>(p.vz, i0, VZ);
         }
     }
     if (kDeposit) run.flush(sbox, box.sx, box.sxy);
