@@ -11,9 +11,8 @@
 // cell index (sort.cu), so the particles of one tile are one contiguous range.
 // One CTA takes (species, tile, part): it stages the tile's node E field plus a
 // halo of `halo` cells into shared memory, zeroes a shared rho box of the same
-// extent, streams its particles with loads and stores coalesced across the
-// warp (one FP64 particle per thread per iteration) and flushes the box to
-// global memory once.  A particle whose cell lies outside the staged box (it
+// extent, streams its particles with 16-byte vector loads and stores (two FP64
+// particles per thread per iteration) and flushes the box to global memory once.  A particle whose cell lies outside the staged box (it
 // drifted since the last sort, or wrapped across the periodic edge) gathers
 // from and deposits to global memory instead.
 //
@@ -38,7 +37,7 @@ namespace ohpic {
 namespace {
 
 constexpr unsigned long long kOne48 = 1ull << 48;
-constexpr int kF64PerThread = 1;
+constexpr int kF64PerThread = 2;
 
 // round(r * 2^48) for r in [0, 1]: r + 16 has its last mantissa bit at 2^-48.
 __device__ __forceinline__ unsigned long long frac48(double r)
@@ -114,10 +113,10 @@ __device__ __forceinline__ void flush_box48(const TileArgs &a, const Item &it, c
 }
 
 // ===========================================================================
-// FP64 form: kF64PerThread consecutive particles per thread per iteration.  One
-// (scalar loads, still coalesced across the warp) keeps the per-thread state
-// within the two-CTA register budget without spills; two (double2 vectors)
-// spilled 124 bytes per thread even with three-component node loads.
+// FP64 form: kF64PerThread consecutive particles per thread per iteration.  Two
+// (double2 vectors) spill 124 bytes per thread at two CTAs per SM; one (scalar
+// loads) spills nothing but issues 38% more instructions and measured slower
+// (220 against 211 ms per step at 256^3).
 // ===========================================================================
 // The three E components of a node (the padded node's fourth is never read).
 struct d3 {
