@@ -268,11 +268,7 @@ void launch_tiled(ohpic_ctx *c, int mode, int strict)
     if (a.sorted) smem = (gather ? s3 * 4 * es : 0) + (dep ? s3 * 8 : 0) + 128;
     // four per lane (FP32 push/deposit): the boxes end on a 16-byte boundary and are
     // followed by the per-thread prefetch stage (7 arrays x 256 threads x 16 bytes)
-    // the FP32 push with a wide halo runs one 512-thread CTA per SM (kWideHalo)
-    const int threads = !f64 && a.ppl == 4 && a.sorted && mode == MODE_PUSH && c->g.halo >= kWideHalo ? kWideThreads
-                                                                                                   : 256;
-    if (!f64 && a.ppl == 4)
-        smem = (a.sorted ? ((s3 * 4 * es + s3 * 8 + 15) & ~(size_t)15) : 0) + kQuadStageBytesPerThread * threads + 128;
+    if (!f64 && a.ppl == 4) smem = (a.sorted ? ((s3 * 4 * es + s3 * 8 + 15) & ~(size_t)15) : 0) + kQuadStageBytes + 128;
     if (f64) {
         launch_tiled_f64(c, a, mode, strict, blocks, smem);
         return;
@@ -284,11 +280,11 @@ void launch_tiled(ohpic_ctx *c, int mode, int strict)
                           a.deposit == OHPIC_DEPOSIT_LANES;
     if (!from_rec) {
         materialize_records(c);
-        launch_tiled_f32(c, a, mode, blocks, smem, nullptr, threads);
+        launch_tiled_f32(c, a, mode, blocks, smem);
         return;
     }
     const RecIn rin{(const int4 *)c->pblock[1 - c->cur], c->ids[c->cur]};
-    launch_tiled_f32(c, a, mode, blocks, smem, &rin, threads);
+    launch_tiled_f32(c, a, mode, blocks, smem, &rin);
     c->rec_pending = false;
 }
 

@@ -63,11 +63,8 @@ bool make_geom(const ohpic_config &k, const int tile[3], int halo, Geom &g)
     // Staged E box (4 reals per node) plus the deposit box (8 bytes per node).
     const int64_t s3 = (int64_t)g.sx * g.sy * g.sz;
     const int64_t es = k.precision == OHPIC_FP64 ? 8 : 4;
-    if (s3 * (4 * es + 8) > 192 * 1024) return false;
-    // the FP32 push adds its prefetch stage: 112 bytes per thread, 512 threads from kWideHalo
-    const int64_t threads = halo >= kWideHalo ? kWideThreads : 256;
-    return k.precision == OHPIC_FP64 ||
-           ((s3 * (4 * es + 8) + 15) & ~15) + (int64_t)kQuadStageBytesPerThread * threads + 128 + 1024 <= 227 * 1024;
+    // (leaves room for the FP32 push's 28 KB prefetch stage within a CTA's 227 KB)
+    return s3 * (4 * es + 8) <= 192 * 1024;
 }
 
 // Boris constants of one species for a time step (particle_mover_boris.f90:37-43),

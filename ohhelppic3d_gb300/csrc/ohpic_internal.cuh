@@ -29,16 +29,10 @@ namespace ohpic {
 constexpr int kSegAlign = 64;       // particles; keeps every species segment 256-B aligned
 constexpr int kMaxHalo = 4;
 // FP32 push with four particles per lane: per-thread prefetch stage in shared memory
-// (7 arrays x 16 bytes per thread; 256 threads per CTA).
-constexpr size_t kQuadStageBytesPerThread = 7 * 16;
-constexpr size_t kQuadStageBytes = kQuadStageBytesPerThread * 256;
+// (7 arrays x 256 threads x 16 bytes).
+constexpr size_t kQuadStageBytes = 7 * 256 * 16;
 // Warps per CTA of the tile kernels (256 threads).
 constexpr int kTileWarps = 8;
-// The FP32 push (four per lane) stages boxes wider than kWideHalo - 1 with one
-// 512-thread CTA per SM instead of two 256-thread CTAs: the box alone would
-// leave room for one CTA, and 16 warps keep the same occupancy.
-constexpr int kWideHalo = 3;
-constexpr int kWideThreads = 512;
 // FP32-form deposit: CIC weights in units of 2^-24 (the 8 weights of a particle sum to exactly 2^24).
 constexpr float kWeightScale = 16777216.0f;
 constexpr double kWeightUnit = 1.0 / 16777216.0;
@@ -297,7 +291,7 @@ void species_consts(const ohpic_config &cfg, int s, double dt, SpeciesConst &k);
 void launch_tiled(ohpic_ctx *c, int mode, int strict);
 void launch_tiled_f64(ohpic_ctx *c, const TileArgs &a, int mode, int strict, int64_t blocks, size_t smem);
 void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks, size_t smem,
-                      const RecIn *rin = nullptr, int threads = 256);
+                      const RecIn *rin = nullptr);
 // FP32 form: turns the sort's pending records back into the word arrays (no-op
 // when none are pending); every entry point that reads or writes particles
 // other than the push that consumes the records calls it first.

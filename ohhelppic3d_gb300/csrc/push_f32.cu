@@ -587,7 +587,7 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
 // the lanes' last sums once per 128 particles.  The per-particle arithmetic is
 // advance(), as in the two-per-lane pass, and every sum is integer, so both
 // passes give the same bits.
-template <int MODE, int DEP, int W, bool REC = false, int NW = kTileWarps>
+template <int MODE, int DEP, int W, bool REC = false>
 __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap,
                                            const Item &it, unsigned char *smem, uint64_t *ebar,
                                            const RecIn &rin = RecIn{})
@@ -693,7 +693,7 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
         __syncthreads();
         flush_f32(a, it, slo, shi);
     }
-    if (kGather) flush_diag<float, NW>(a, sp, t.cx, t.cy, t.cz, t.out, t.ke, t.px, t.py, t.pz);
+    if (kGather) flush_diag<float>(a, sp, t.cx, t.cy, t.cz, t.out, t.ke, t.px, t.py, t.pz);
 }
 
 __device__ __forceinline__ unsigned char *align128(unsigned char *p)
@@ -724,30 +724,17 @@ __global__ void __launch_bounds__(256, 2) tiled_f32(TileArgs a, PartF32 p, const
     run_item<MODE, DEP, PPL, W>(a, p, &emap, (int64_t)blockIdx.x, align128(smem_raw), &ebar);
 }
 
-// The same with one 512-thread CTA per SM, for halos of kWideHalo and more.
-template <int DEP, int W>
-__global__ void __launch_bounds__(kWideThreads, 1) tiled_f32_wide(TileArgs a, PartF32 p,
-                                                                 const __grid_constant__ CUtensorMap emap)
-{
-    extern __shared__ unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t ebar;
-    Item it;
-    if (get_item<4>(a, (int64_t)blockIdx.x, it))
-        tile_pass4<MODE_PUSH, DEP, W, false, kWideThreads / 32>(a, p, &emap, it, align128(smem_raw), &ebar);
-}
-
 // The push right after a sort, reading the sort's records (four per lane, LANES
 // deposit: the default launch shape); writes the word arrays p and the ids.
-template <int W, int NT>
-__global__ void __launch_bounds__(NT, 512 / NT) tiled_f32_rec(TileArgs a, PartF32 p, RecIn rin,
-                                                             const __grid_constant__ CUtensorMap emap)
+template <int W>
+__global__ void __launch_bounds__(256, 2) tiled_f32_rec(TileArgs a, PartF32 p, RecIn rin,
+                                                        const __grid_constant__ CUtensorMap emap)
 {
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t ebar;
     Item it;
     if (get_item<4>(a, (int64_t)blockIdx.x, it))
-        tile_pass4<MODE_PUSH, OHPIC_DEPOSIT_LANES, W, true, NT / 32>(a, p, &emap, it, align128(smem_raw), &ebar,
-                                                                      rin);
+        tile_pass4<MODE_PUSH, OHPIC_DEPOSIT_LANES, W, true>(a, p, &emap, it, align128(smem_raw), &ebar, rin);
 }
 
 // Many contexts in one persistent launch.  Every CTA takes the next item from
@@ -808,14 +795,14 @@ __global__ void __launch_bounds__(256, 2) tiled_f32_multi(MultiPush m)
 
 template <typename P>
 static void launch_k(ohpic_ctx *c, void (*kernel)(TileArgs, P, const CUtensorMap), const TileArgs &a,
-                     int64_t blocks, size_t smem, const P &parts, int threads = 256)
+                     int64_t blocks, size_t smem, const P &parts)
 {
     if (blocks <= 0) return;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     // CTAs over ~96 KB pair up on an SM only with the whole shared-memory carveout
     if (smem > 96 * 1024)
         cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-    kernel<<<(unsigned)blocks, threads, smem, c->stream>>>(a, parts, c->emap);
+    kernel<<<(unsigned)blocks, 256, smem, c->stream>>>(a, parts, c->emap);
     ++c->launches;
 }
 
@@ -847,29 +834,20 @@ static auto by_weights(int w, F f)
     return f(std::integral_constant<int, OHPIC_WEIGHTS_STANDARD>());
 }
 
-void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks, size_t smem, const RecIn *rin,
-                      int threads)
+void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks, size_t smem, const RecIn *rin)
 {
     const PartF32 &pp = c->p32[c->cur];
     by_weights(a.weights, [&](auto w) {
         constexpr int W = decltype(w)::value;
         if (rin) {
             if (blocks <= 0) return 0;
-            auto kernel = threads == kWideThreads ? tiled_f32_rec<W, kWideThreads> : tiled_f32_rec<W, 256>;
+            auto kernel = tiled_f32_rec<W>;
             cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (smem > 96 * 1024)
                 cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                      cudaSharedmemCarveoutMaxShared);
-            kernel<<<(unsigned)blocks, threads, smem, c->stream>>>(a, pp, *rin, c->emap);
+            kernel<<<(unsigned)blocks, 256, smem, c->stream>>>(a, pp, *rin, c->emap);
             ++c->launches;
-            return 0;
-        }
-        if (mode == MODE_PUSH && threads == kWideThreads) {
-            by_deposit(a.deposit, [&](auto d) {
-                constexpr int D = decltype(d)::value;
-                launch_k(c, tiled_f32_wide<D, W>, a, blocks, smem, pp, kWideThreads);
-                return 0;
-            });
             return 0;
         }
         if (mode == MODE_PUSH || mode == MODE_DEPOSIT) {

@@ -265,25 +265,25 @@ __device__ __forceinline__ void load_nodes(const TileArgs &a, const Box &b, int 
     }
 }
 
-// Block-wide reduction of the per-thread diagnostics into DevDiag.  NW is the
-// CTA's warp count: the tile kernels run 256 threads (8 warps), and the scratch
-// is sized for exactly that (512 bytes of static shared memory keep a CTA with
-// a (16,8,8) tile at halo 2 within two CTAs per SM); the wide FP32 push runs 16.
-template <typename T, int NW = kTileWarps>
+// Block-wide reduction of the per-thread diagnostics into DevDiag.
+template <typename T>
 __device__ void flush_diag(const TileArgs &a, int sp, unsigned cx, unsigned cy, unsigned cz, unsigned outside, T ke,
                            T px, T py, T pz)
 {
-    __shared__ double red[8][NW];
+    // The tile kernels run 256 threads (8 warps).  The scratch is sized for
+    // exactly that: 512 bytes of static shared memory keep a CTA with a
+    // (16,8,8) tile at halo 2 within two CTAs per SM.
+    __shared__ double red[8][kTileWarps];
     double v[8] = {(double)cx, (double)cy, (double)cz, (double)outside, (double)ke, (double)px, (double)py, (double)pz};
 #pragma unroll
     for (int k = 0; k < 8; ++k)
         for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(kFull, v[k], o);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0 && warp < NW)
+    if (lane == 0 && warp < kTileWarps)
         for (int k = 0; k < 8; ++k) red[k][warp] = v[k];
     __syncthreads();
     if (warp == 0) {
-        const int nw = min((int)(blockDim.x >> 5), NW);
+        const int nw = min((int)(blockDim.x >> 5), kTileWarps);
         for (int k = 0; k < 8; ++k) {
             double s = lane < nw ? red[k][lane] : 0.0;
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(kFull, s, o);
