@@ -39,10 +39,59 @@ namespace {
 constexpr unsigned long long kOne48 = 1ull << 48;
 constexpr int kF64PerThread = 2;
 
-// round(r * 2^48) for r in [0, 1]: r + 16 has its last mantissa bit at 2^-48.
-__device__ __forceinline__ unsigned long long frac48(double r)
+// Cell index and in-cell offset of a coordinate by integer operations on its
+// bit pattern.  On GB300 the FP64 pipe bounds this form, and (int)x,
+// (double)ix, x - ix and the 48-bit rounding were six of its operations per axis.
+// A coordinate is kept as (fr, e): for x >= 1, e is its binary exponent and fr
+// the mantissa bits below the binary point, so the offset is fr * 2^(e-52); for
+// x in [0, 1) (and -0.0), e = -1 and fr holds the bits of x itself.
+struct Split {
+    unsigned long long fr;
+    int e;
+};
+
+// floor(x) for x in [0, 2^30); -1 for anything else (negative, NaN, too large).
+__device__ __forceinline__ int split_cell(double x, Split &s)
 {
-    return (unsigned long long)__double_as_longlong(r + 16.0) & ((1ull << 52) - 1);
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int E = (int)(b >> 52);                       // the sign bit makes negatives >= 2048
+    if (E < 1023 || b == 0x8000000000000000ull) {       // [0, 1) and -0.0: cell 0, offset x
+        s.fr = b;
+        s.e = -1;
+        return 0;
+    }
+    s.e = E - 1023;
+    if (s.e > 29) return -1;
+    const unsigned long long F = (b & ((1ull << 52) - 1)) | (1ull << 52);
+    const int sh = 52 - s.e;
+    s.fr = F & ((1ull << sh) - 1);
+    return (int)(F >> sh);
+}
+
+// The offset x - floor(x) as a double, exact (the same bits FP64 subtraction gives).
+__device__ __forceinline__ double split_frac(const Split &s)
+{
+    if (s.e < 0) return __longlong_as_double((long long)s.fr);
+    if (s.fr == 0) return 0.0;
+    const int p = 63 - __clzll((long long)s.fr);       // top set bit; the value is 2^(p+e-52) * 1.m
+    const unsigned long long mant = (s.fr << (52 - p)) & ((1ull << 52) - 1);
+    return __longlong_as_double((long long)(((unsigned long long)(p + s.e + 971) << 52) | mant));
+}
+
+// round(offset * 2^48), ties up.
+__device__ __forceinline__ unsigned long long split_frac48(const Split &s)
+{
+    if (s.e >= 4) return s.fr << (s.e - 4);
+    if (s.e >= 0) {
+        const int sh = 4 - s.e;
+        return (s.fr + (1ull << (sh - 1))) >> sh;
+    }
+    const int E = (int)((s.fr >> 52) & 0x7ff);           // x in [0, 1): x * 2^48 = F * 2^(E - 1027)
+    if (E == 0) return 0;
+    const int sh = 1027 - E;                            // >= 5
+    if (sh > 54) return 0;
+    const unsigned long long F = (s.fr & ((1ull << 52) - 1)) | (1ull << 52);
+    return (F + (1ull << (sh - 1))) >> sh;
 }
 
 // round(p * w / 2^48) for p, w <= 2^48, from the 96-bit product.
@@ -53,11 +102,11 @@ __device__ __forceinline__ unsigned long long mul48(unsigned long long p, unsign
     return q + ((lo >> 47) & 1ull);
 }
 
-// The 8 weights of a particle with offsets rx, ry, rz in [0, 1), in units of
-// 2^-48, summing to exactly 2^48; order x fastest as in add8 / deposit_global.
-__device__ __forceinline__ void fixed_weights48(int conv, double rx, double ry, double rz, unsigned long long u[8])
+// The 8 weights of a particle whose offsets are Rx, Ry, Rz (units of 2^-48), in
+// units of 2^-48, summing to exactly 2^48; order x fastest as in add8 / deposit_global.
+__device__ __forceinline__ void fixed_weights48(int conv, unsigned long long Rx, unsigned long long Ry,
+                                                unsigned long long Rz, unsigned long long u[8])
 {
-    const unsigned long long Rx = frac48(rx), Ry = frac48(ry), Rz = frac48(rz);
     const bool ref = conv == OHPIC_WEIGHTS_REFERENCE;   // node floor(x) takes r (linear_scatter.f90:41-42)
     const unsigned long long X1 = ref ? kOne48 - Rx : Rx, X0 = kOne48 - X1;
     const unsigned long long wy1 = ref ? kOne48 - Ry : Ry, wz1 = ref ? kOne48 - Rz : Rz;
@@ -234,7 +283,8 @@ __global__ void __launch_bounds__(256, 2) tiled_f64(TileArgs a, PartF64 p)
             if (i0 + j >= end) continue;
             double x = X[j], y = Y[j], z = Z[j];
             if (kGather) {
-                const int ix = (int)x, iy = (int)y, iz = (int)z;
+                Split sx_, sy_, sz_;
+                const int ix = split_cell(x, sx_), iy = split_cell(y, sy_), iz = split_cell(z, sz_);
                 if ((unsigned)ix >= (unsigned)g.nx || (unsigned)iy >= (unsigned)g.ny ||
                     (unsigned)iz >= (unsigned)g.nz) {
                     flag_error(a.diag, OHPIC_ERR_BOUNDS, 1);
@@ -245,9 +295,10 @@ __global__ void __launch_bounds__(256, 2) tiled_f64(TileArgs a, PartF64 p)
                 d3 nd[8];
                 load_nodes3(a, box, key, ix, iy, iz, sE, nd);
                 double wx0, wx1, wy0, wy1, wz0, wz1;
-                cic<double>(a.weights, Ops::sub(x, (double)ix), wx0, wx1);
-                cic<double>(a.weights, Ops::sub(y, (double)iy), wy0, wy1);
-                cic<double>(a.weights, Ops::sub(z, (double)iz), wz0, wz1);
+                // x - floor(x) exactly (linear_interpolator.f90:47-52), from the bits
+                cic<double>(a.weights, split_frac(sx_), wx0, wx1);
+                cic<double>(a.weights, split_frac(sy_), wy0, wy1);
+                cic<double>(a.weights, split_frac(sz_), wz0, wz1);
                 double ex, ey, ez;
                 if (STRICT) {
                     // ret = ret + v*rx*ry*rz, i (x) outermost (linear_interpolator.f90:62-66).
@@ -325,7 +376,8 @@ __global__ void __launch_bounds__(256, 2) tiled_f64(TileArgs a, PartF64 p)
                 }
             }
             if (kDeposit) {
-                const int jx = (int)x, jy = (int)y, jz = (int)z;
+                Split tx_, ty_, tz_;
+                const int jx = split_cell(x, tx_), jy = split_cell(y, ty_), jz = split_cell(z, tz_);
                 if ((unsigned)jx >= (unsigned)g.nx || (unsigned)jy >= (unsigned)g.ny ||
                     (unsigned)jz >= (unsigned)g.nz) {
                     flag_error(a.diag, OHPIC_ERR_BOUNDS, 2);
@@ -334,7 +386,7 @@ __global__ void __launch_bounds__(256, 2) tiled_f64(TileArgs a, PartF64 p)
                 // rx*ry*rz of linear_scatter.f90:41-52 in 2^-48 fixed point; the
                 // charge amount is applied per species when rho is formed
                 unsigned long long w[8];
-                fixed_weights48(a.weights, x - (double)jx, y - (double)jy, z - (double)jz, w);
+                fixed_weights48(a.weights, split_frac48(tx_), split_frac48(ty_), split_frac48(tz_), w);
                 const int key = box.key(jx, jy, jz);
                 if (key >= 0) {
                     run.add(key, w, sbox, box.sx, box.sxy);
