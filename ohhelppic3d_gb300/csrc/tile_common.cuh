@@ -265,41 +265,60 @@ __device__ __forceinline__ void load_nodes(const TileArgs &a, const Box &b, int 
     }
 }
 
-// Block-wide reduction of the per-thread diagnostics into DevDiag.
+// Block-wide reduction of the per-thread diagnostics into DevDiag.  The counts
+// reduce with integer warp reductions; the kinetic sums (in FP64, converted per
+// thread) only when the push tracks them.  On GB300 an FP64 add runs on the narrow
+// FP64 pipe, and reducing all eight tallies in FP64 at the end of every work item
+// kept that pipe 4.5% busy in the FP32 push.
 template <typename T>
 __device__ void flush_diag(const TileArgs &a, int sp, unsigned cx, unsigned cy, unsigned cz, unsigned outside, T ke,
                            T px, T py, T pz)
 {
-    // The tile kernels run 256 threads (8 warps).  The scratch is sized for
-    // exactly that: 512 bytes of static shared memory keep a CTA with a
-    // (16,8,8) tile at halo 2 within two CTAs per SM.
-    __shared__ double red[8][kTileWarps];
-    double v[8] = {(double)cx, (double)cy, (double)cz, (double)outside, (double)ke, (double)px, (double)py, (double)pz};
+    // The tile kernels run 256 threads (8 warps); the scratch is sized for exactly
+    // that and keeps the static shared memory of a (16,8,8) tile at halo 2 within
+    // two CTAs per SM.
+    __shared__ unsigned cnt[4][kTileWarps];
+    __shared__ double kin[4][kTileWarps];
+    const bool energy = a.with_energy != 0;
+    unsigned u[4] = {cx, cy, cz, outside};
 #pragma unroll
-    for (int k = 0; k < 8; ++k)
-        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(kFull, v[k], o);
+    for (int k = 0; k < 4; ++k) u[k] = __reduce_add_sync(kFull, u[k]);
+    double v[4] = {(double)ke, (double)px, (double)py, (double)pz};
+    if (energy) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(kFull, v[k], o);
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0 && warp < kTileWarps)
-        for (int k = 0; k < 8; ++k) red[k][warp] = v[k];
+    if (lane == 0 && warp < kTileWarps) {
+        for (int k = 0; k < 4; ++k) {
+            cnt[k][warp] = u[k];
+            kin[k][warp] = v[k];
+        }
+    }
     __syncthreads();
     if (warp == 0) {
         const int nw = min((int)(blockDim.x >> 5), kTileWarps);
-        for (int k = 0; k < 8; ++k) {
-            double s = lane < nw ? red[k][lane] : 0.0;
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(kFull, s, o);
-            v[k] = s;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) u[k] = __reduce_add_sync(kFull, lane < nw ? cnt[k][lane] : 0u);
+        if (energy) {
+            for (int k = 0; k < 4; ++k) {
+                double t = lane < nw ? kin[k][lane] : 0.0;
+                for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(kFull, t, o);
+                v[k] = t;
+            }
         }
         if (lane == 0) {
             DevDiag *d = a.diag;
-            if (v[0] != 0.0) atomicAdd(&d->crossings[0], (unsigned long long)v[0]);
-            if (v[1] != 0.0) atomicAdd(&d->crossings[1], (unsigned long long)v[1]);
-            if (v[2] != 0.0) atomicAdd(&d->crossings[2], (unsigned long long)v[2]);
-            if (v[3] != 0.0) atomicAdd(&d->outside, (unsigned long long)v[3]);
-            if (a.with_energy) {
-                atomicAdd(&d->kin[sp][0], v[4]);
-                atomicAdd(&d->kin[sp][1], v[5]);
-                atomicAdd(&d->kin[sp][2], v[6]);
-                atomicAdd(&d->kin[sp][3], v[7]);
+            if (u[0]) atomicAdd(&d->crossings[0], (unsigned long long)u[0]);
+            if (u[1]) atomicAdd(&d->crossings[1], (unsigned long long)u[1]);
+            if (u[2]) atomicAdd(&d->crossings[2], (unsigned long long)u[2]);
+            if (u[3]) atomicAdd(&d->outside, (unsigned long long)u[3]);
+            if (energy) {
+                atomicAdd(&d->kin[sp][0], v[0]);
+                atomicAdd(&d->kin[sp][1], v[1]);
+                atomicAdd(&d->kin[sp][2], v[2]);
+                atomicAdd(&d->kin[sp][3], v[3]);
             }
         }
     }
