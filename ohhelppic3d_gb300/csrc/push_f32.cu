@@ -346,26 +346,45 @@ __device__ __forceinline__ void read_quad(const float4 *st, P32 r[4])
 // a0 b0 a1 b1 a2 b2 a3 b3 (a = cell and offsets, b = velocities and id); the
 // first seven go through the stage slots the seven arrays use, and b3 is
 // loaded into registers one quad ahead.
-__device__ __forceinline__ void prefetch_rec(float4 *st, const int4 *rec, int64_t g)
+//
+// The warp stages its 32 quads together, as rows of the seven staged halves
+// (112 bytes per quad, the warp's 3.5 KB where the arrays' seven slots per
+// thread would be).  In copy k, lane l takes half t = l & 7 of quad
+// 4k + (l >> 3), so a copy instruction reads one 512-byte span of records and
+// its 28 active lanes write 448 contiguous bytes of the stage; lanes with t = 7
+// (a b3 half) sit out.  A thread then reads its own row: rows of seven 16-byte
+// slots put the eight lanes of a quarter-warp in eight different bank groups.
+// Every lane of the warp runs this; quads at or past g1 are skipped.
+__device__ __forceinline__ void prefetch_rec_warp(float4 *st, const int4 *rec, int64_t base, int64_t g1)
 {
-    const int n = blockDim.x, i = threadIdx.x;
-    const int4 *q = rec + 8 * g;
+    const int lane = (int)(threadIdx.x & 31u), first = (int)(threadIdx.x & ~31u);
+    const int t = lane & 7;
+    const int64_t wq = base + first;          // the warp's first quad
+    float4 *rows = st + 7 * first;
+    if (t != 7) {
 #pragma unroll
-    for (int k = 0; k < 7; ++k) cp_async16(st + k * n + i, q + k);
+        for (int k = 0; k < 8; ++k) {
+            const int o = 4 * k + (lane >> 3);
+            if (wq + o < g1) cp_async16(rows + 7 * o + t, rec + 8 * (wq + o) + t);
+        }
+    }
     asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
+// The thread's row was filled by other lanes of its warp: every lane waits for
+// its own copies, then the warp barrier makes them visible across the warp.
 __device__ __forceinline__ void read_rec(const float4 *st, const int4 &b3, P32 r[4], uint4 &id)
 {
     asm volatile("cp.async.wait_group 0;" ::: "memory");
-    const int n = blockDim.x, i = threadIdx.x;
+    __syncwarp();
+    const float4 *row = st + 7 * threadIdx.x;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        const float4 a = st[2 * j * n + i];
+        const float4 a = row[2 * j];
         r[j].cell = __float_as_int(a.x);
         r[j].ox = a.y; r[j].oy = a.z; r[j].oz = a.w;
     }
-    const float4 b0 = st[n + i], b1 = st[3 * n + i], b2 = st[5 * n + i];
+    const float4 b0 = row[1], b1 = row[3], b2 = row[5];
     r[0].vx = b0.x; r[0].vy = b0.y; r[0].vz = b0.z;
     r[1].vx = b1.x; r[1].vy = b1.y; r[1].vz = b1.z;
     r[2].vx = b2.x; r[2].vy = b2.y; r[2].vz = b2.z;
@@ -633,13 +652,11 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
     const size_t boxes = box.on ? ((kGather ? (size_t)s3 * sizeof(float4) : 0) + (size_t)s3 * 8 + 15) & ~(size_t)15 : 0;
     float4 *stage = (float4 *)(smem + boxes);
     int4 b3 = make_int4(0, 0, 0, 0);   // REC: the current quad's last record half
-    if (it.g0 + threadIdx.x < it.g1) {
-        if (REC) {
-            prefetch_rec(stage, rin.rec, it.g0 + threadIdx.x);
-            b3 = __ldg(rin.rec + 8 * (it.g0 + threadIdx.x) + 7);
-        } else {
-            prefetch_quad<kGather>(stage, p, it.g0 + threadIdx.x);
-        }
+    if (REC) {
+        prefetch_rec_warp(stage, rin.rec, it.g0, it.g1);
+        if (it.g0 + threadIdx.x < it.g1) b3 = __ldg(rin.rec + 8 * (it.g0 + threadIdx.x) + 7);
+    } else if (it.g0 + threadIdx.x < it.g1) {
+        prefetch_quad<kGather>(stage, p, it.g0 + threadIdx.x);
     }
 
     for (int64_t base = it.g0; base < it.g1; base += blockDim.x) {
@@ -648,17 +665,19 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
         unsigned acc[8];
 #pragma unroll
         for (int v = 0; v < 8; ++v) acc[v] = 0u;
+        P32 q[4];
+        uint4 qid;
+        int4 b3_next = make_int4(0, 0, 0, 0);
+        if (REC) {
+            // the whole warp: its lanes read each other's copies, and the next
+            // copies overwrite the stage only after every lane has read it
+            read_rec(stage, b3, q, qid);
+            __syncwarp();
+            if (base + blockDim.x < it.g1) prefetch_rec_warp(stage, rin.rec, base + blockDim.x, it.g1);
+            if (gi + blockDim.x < it.g1) b3_next = __ldg(rin.rec + 8 * (gi + blockDim.x) + 7);
+        }
         if (gi < it.g1) {
-            P32 q[4];
-            uint4 qid;
-            int4 b3_next = make_int4(0, 0, 0, 0);
-            if (REC) {
-                read_rec(stage, b3, q, qid);
-                if (gi + blockDim.x < it.g1) {
-                    prefetch_rec(stage, rin.rec, gi + blockDim.x);
-                    b3_next = __ldg(rin.rec + 8 * (gi + blockDim.x) + 7);
-                }
-            } else {
+            if (!REC) {
                 read_quad<kGather>(stage, q);
                 if (gi + blockDim.x < it.g1) prefetch_quad<kGather>(stage, p, gi + blockDim.x);
             }
