@@ -79,18 +79,40 @@ __device__ __forceinline__ uint32_t particle_key(const Geom &g, const uint32_t *
     return cell_key(g, tab, (int)p64.x[i], (int)p64.y[i], (int)p64.z[i], d);
 }
 
-// Warp-aggregated atomicAdd of 1 per lane on count[key]; returns this lane's slot.
-__device__ __forceinline__ uint32_t aggregated_inc(uint32_t *count, uint32_t key, bool active)
+// Warp-aggregated atomicAdd of 1 per lane on count[key], in two halves so a
+// thread can have several in flight: agg_issue groups the lanes by key and lets
+// each group's leader add the group's size; agg_slot (after every issue the
+// thread has in flight) broadcasts the leader's old count and returns this
+// lane's slot.
+struct Agg {
+    unsigned peers;
+    int leader;
+    uint32_t base;
+};
+
+__device__ __forceinline__ void agg_issue(uint32_t *count, uint32_t key, bool active, Agg &a)
 {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned act = __ballot_sync(kFull, active);
     const uint32_t k = active ? key : 0xffffffffu - lane;
-    const unsigned peers = __match_any_sync(kFull, k) & act;
-    uint32_t base = 0;
-    const int leader = peers ? __ffs(peers) - 1 : -1;
-    if (active && (int)lane == leader) base = atomicAdd(count + key, (uint32_t)__popc(peers));
-    base = __shfl_sync(kFull, base, leader < 0 ? (int)lane : leader);
-    return base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+    a.peers = __match_any_sync(kFull, k) & act;
+    a.leader = a.peers ? __ffs(a.peers) - 1 : -1;
+    a.base = 0;
+    if (active && (int)lane == a.leader) a.base = atomicAdd(count + key, (uint32_t)__popc(a.peers));
+}
+
+__device__ __forceinline__ uint32_t agg_slot(const Agg &a)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t base = __shfl_sync(kFull, a.base, a.leader < 0 ? (int)lane : a.leader);
+    return base + (uint32_t)__popc(a.peers & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ uint32_t aggregated_inc(uint32_t *count, uint32_t key, bool active)
+{
+    Agg a;
+    agg_issue(count, key, active, a);
+    return agg_slot(a);
 }
 
 // Histogram add of 1 per active lane, one atomic per run of adjacent lanes with
@@ -110,10 +132,11 @@ __device__ __forceinline__ void run_count(uint32_t *count, uint32_t key, bool ac
 
 // The sort kernels are bound by memory latency (a cell load, then an atomic, then
 // the record), so each thread keeps several independent particles in flight:
-// four per iteration in the histogram, two in the scatter, whose record loads are
-// all issued before the atomics.  Launch bounds keep enough warps resident: five
-// CTAs of 256 per SM for the histogram, four for the FP32 scatter (64 registers,
-// against 70 and three CTAs without the bound).
+// four per iteration in the histogram; in the FP32 scatter four, whose record
+// loads are all issued first and whose cursor atomics are all in flight before
+// the first result is used (two in the FP64 scatter).  Launch bounds keep enough
+// warps resident: five CTAs of 256 per SM for the histogram, three for the FP32
+// scatter.
 template <bool F32>
 __global__ void __launch_bounds__(256, 5) k_hist(Geom g, const uint32_t *tab, PartF64 p64, PartF32 p32, int64_t seg, int64_t n,
                        uint32_t *count, DevDiag *d)
@@ -195,8 +218,11 @@ __global__ void __launch_bounds__(256, 4) k_scatter_rec32(Geom g, const uint32_t
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) key[u] = act[u] ? rec_key<true>(g, tab, r[u], d) : 0u;
+        Agg agg[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u) slot[u] = aggregated_inc(cursor, key[u], act[u]);
+        for (int u = 0; u < U; ++u) agg_issue(cursor, key[u], act[u], agg[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u) slot[u] = agg_slot(agg[u]);
 #pragma unroll
         for (int u = 0; u < U; ++u)
             if (act[u]) rec32_store(rec, seg + (int64_t)start[key[u]] + slot[u], r[u]);
