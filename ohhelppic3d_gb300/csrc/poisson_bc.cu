@@ -18,10 +18,19 @@
 //   DCT-III:            DFT of length 2L of u_m e^{-i pi m/2L} (u: x_0, x_1.., 0, -x_{L-1}.., -x_1)
 //   DST-II:             DCT-II of (-1)^j x_j, read in reverse order
 //   DST-III:            (-1)^k DCT-III of the reversed line
-//   periodic:           forward and inverse DFT of length L (the same operator as
-//                       FFTW's separable R2HC/HC2R for a Poisson solve).
-// The working array is complex, so every transform applies to real and
-// imaginary parts alike (they are all linear), whatever order the axes come in.
+//   R2HC:               DFT of length L, split into the two real lines' spectra
+//                       (F_A = (Z_k + conj Z_{L-k}) / 2, F_B = (Z_k - conj Z_{L-k}) / 2i)
+//                       and stored half-complex (Re F_k at k <= L/2, Im F_k at L-k)
+//   HC2R:               the two half-complex lines combined into G = F_A + i F_B,
+//                       inverse DFT of length L: its real part is line A's, its
+//                       imaginary part line B's.
+// Two real lines per complex transform.  The working array R is real, and every
+// transform above maps a real line to a real line and is linear, so one complex
+// transform carries two lines: line A in the real part and line B, its partner
+// half a block away along another axis (the pack axis), in the imaginary part.
+// The DCT/DST forms are complex-linear as they stand; R2HC and HC2R separate and
+// combine the pair explicitly.  Each pass therefore runs half the lines of
+// cuFFT work and moves half the extension bytes of a complex working array.
 // Every extension is stored line-contiguous, so cuFFT runs contiguous batched
 // transforms on every axis; along y and z the extension and extraction kernels
 // transpose 32 x 32 tiles through shared memory so that both their reads and
@@ -45,7 +54,7 @@ namespace {
 // The reference's pi literal (src/utils/science_constants.f90:4) for the tables.
 constexpr double kRefPi = 3.14159265358979;
 
-enum Xform { XF_DFT, XF_IDFT, XF_DCT1, XF_DST1, XF_DCT2, XF_DCT3, XF_DST2, XF_DST3 };
+enum Xform { XF_R2HC, XF_HC2R, XF_DCT1, XF_DST1, XF_DCT2, XF_DCT3, XF_DST2, XF_DST3 };
 
 struct Axis {
     int kind;        // OHPIC_BC_*
@@ -66,7 +75,7 @@ bool make_axis(int kind, int n, Axis &a)
     a.wall_lo = a.wall_hi = false;
     switch (kind) {
     case OHPIC_BC_PERIODIC:
-        a.fwd = XF_DFT; a.bwd = XF_IDFT; a.ls = 0; a.L = n; a.M = a.L; a.norm = (double)a.L;
+        a.fwd = XF_R2HC; a.bwd = XF_HC2R; a.ls = 0; a.L = n; a.M = a.L; a.norm = (double)a.L;
         break;
     case OHPIC_BC_DIRICHLET:
         a.fwd = a.bwd = XF_DST1; a.ls = 1; a.L = n - 1; a.M = 2 * (a.L + 1); a.norm = 2.0 * (a.L + 1.0);
@@ -117,22 +126,53 @@ double eigenvalue(int i, int n, int kind)
     }
 }
 
-// Lines of one axis of an (L0, L1, L2) array, x fastest.
+// Lines of one axis of the real (L0, L1, L2) array R, x fastest, in pairs: the
+// packed extents P equal L except along the pack axis, where P = H = ceil(L / 2)
+// and the element at pack coordinate c is paired with the one at c + H (none
+// when c + H is past the end: its half of the pair is zero and not stored).
+// Lines are numbered over the packed extents of the two other axes, the lower
+// axis fastest, so consecutive lines are consecutive in memory along y and z.
 struct Lines {
-    int axis;
-    int L0, L1, L2;
+    int axis, pack;
+    int P0, P1, P2;          // packed extents
+    int L0, L1;              // R's x and y extents (its strides)
+    int H, Lp;               // pack offset and R's extent along the pack axis
+    int64_t pstride;         // R distance from an element to its partner
     int64_t lines;
     int M;
 };
 
-__device__ __forceinline__ int64_t w_index(const Lines &m, int64_t line, int j)
+// R index of element j of line `line` (the pair's first half); pair: the
+// partner exists.
+__device__ __forceinline__ int64_t r_index(const Lines &m, int64_t line, int j, bool &pair)
 {
-    if (m.axis == 0) return j + (int64_t)m.L0 * line;
-    if (m.axis == 1) {
-        const int64_t x = line % m.L0, z = line / m.L0;
-        return x + (int64_t)m.L0 * (j + (int64_t)m.L1 * z);
+    int64_t c0, c1, c2;
+    if (m.axis == 0) {
+        c0 = j; c1 = line % m.P1; c2 = line / m.P1;
+    } else if (m.axis == 1) {
+        c0 = line % m.P0; c1 = j; c2 = line / m.P0;
+    } else {
+        c0 = line % m.P0; c1 = line / m.P0; c2 = j;
     }
-    return line + (int64_t)m.L0 * m.L1 * j;
+    const int64_t cp = m.pack == 0 ? c0 : (m.pack == 1 ? c1 : c2);
+    pair = cp + m.H < m.Lp;
+    return c0 + (int64_t)m.L0 * (c1 + (int64_t)m.L1 * c2);
+}
+
+// Element j of line `line` as a complex pair (line A, line B).
+__device__ __forceinline__ double2 load_pair(const Lines &m, const double *R, int64_t line, int j)
+{
+    bool pair;
+    const int64_t i = r_index(m, line, j, pair);
+    return make_double2(R[i], pair ? R[i + m.pstride] : 0.0);
+}
+
+__device__ __forceinline__ void store_pair(const Lines &m, double *R, int64_t line, int j, double2 v)
+{
+    bool pair;
+    const int64_t i = r_index(m, line, j, pair);
+    R[i] = v.x;
+    if (pair) R[i + m.pstride] = v.y;
 }
 
 // (a + ib) e^{-i pi num / den}
@@ -144,14 +184,21 @@ __device__ __forceinline__ double2 rotate(double2 v, double num, double den)
 }
 
 // Extension element mi of line `line` for transform xf (see the header).
-__device__ __forceinline__ double2 ext_value(const Lines &m, int xf, int L, const double2 *W, int64_t line, int mi)
+__device__ __forceinline__ double2 ext_value(const Lines &m, int xf, int L, const double *R, int64_t line, int mi)
 {
+    if (xf == XF_HC2R) {
+        // G_k = F_A,k + i F_B,k from the half-complex pairs at k and L - k
+        const int kk = mi == 0 ? 0 : L - mi;
+        const double2 p = load_pair(m, R, line, mi);
+        if (kk == mi) return p;   // k = 0, and k = L/2 for even L: real spectra
+        const double2 q = load_pair(m, R, line, kk);
+        return mi < kk ? make_double2(p.x - q.y, q.x + p.y) : make_double2(q.x + p.y, q.y - p.x);
+    }
     int j = -1;
     double sgn = 1.0;
     bool twiddle = false;
     switch (xf) {
-    case XF_DFT:
-    case XF_IDFT: j = mi; break;
+    case XF_R2HC: j = mi; break;
     case XF_DCT1: j = mi < L ? mi : m.M - mi; break;
     case XF_DST1:
         if (mi == 0 || mi == L + 1) j = -1;
@@ -173,7 +220,7 @@ __device__ __forceinline__ double2 ext_value(const Lines &m, int xf, int L, cons
     }
     double2 v = make_double2(0.0, 0.0);
     if (j >= 0) {
-        v = W[w_index(m, line, j)];
+        v = load_pair(m, R, line, j);
         v.x *= sgn;
         v.y *= sgn;
     }
@@ -198,39 +245,46 @@ __device__ __forceinline__ double2 extract_value(int xf, int L, const double2 *Z
         const double2 z = Z[k];
         return (k & 1) ? make_double2(-z.x, -z.y) : z;
     }
-    default: return Z[k];   // DFT, IDFT, DCT1, DCT3
+    case XF_R2HC: {
+        // the pair's spectra at k and L - k, stored half-complex
+        const int kk = k == 0 ? 0 : L - k;
+        const double2 z = Z[k], w = Z[kk];
+        if (k <= kk) return make_double2(0.5 * (z.x + w.x), 0.5 * (z.y + w.y));   // Re F_A,k, Re F_B,k
+        return make_double2(0.5 * (w.y - z.y), 0.5 * (z.x - w.x));               // Im F_A,L-k, Im F_B,L-k
+    }
+    default: return Z[k];   // HC2R, DCT1, DCT3
     }
 }
 
 // Every extension is stored line-contiguous, B[line * M + mi], so one batched
-// cuFFT plan of contiguous transforms serves every axis.  Along x the lines of W
+// cuFFT plan of contiguous transforms serves every axis.  Along x the lines of R
 // are contiguous too and a thread per (line, mi) reads and writes coalesced.
-// Along y and z consecutive lines are consecutive in W instead, so 32 x 32
+// Along y and z consecutive lines are consecutive in R instead, so 32 x 32
 // tiles go through shared memory: reads run along lines, writes along mi.
 constexpr int kTile = 32, kTileRows = 8;
 
-__global__ void k_extend_x(Lines m, int xf, int L, const double2 *W, double2 *B)
+__global__ void k_extend_x(Lines m, int xf, int L, const double *R, double2 *B)
 {
     const int64_t total = (int64_t)m.M * m.lines;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t line = t / m.M;
         const int mi = (int)(t - line * m.M);
-        B[t] = ext_value(m, xf, L, W, line, mi);
+        B[t] = ext_value(m, xf, L, R, line, mi);
     }
 }
 
-__global__ void k_extract_x(Lines m, int xf, int L, const double2 *B, double2 *W)
+__global__ void k_extract_x(Lines m, int xf, int L, const double2 *B, double *R)
 {
     const int64_t total = (int64_t)L * m.lines;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t line = t / L;
         const int k = (int)(t - line * L);
-        W[w_index(m, line, k)] = extract_value(xf, L, B + line * m.M, k);
+        store_pair(m, R, line, k, extract_value(xf, L, B + line * m.M, k));
     }
 }
 
 // grid (ceil(lines / 32), ceil(M / 32)), block (32, 8)
-__global__ void k_extend_yz(Lines m, int xf, int L, const double2 *W, double2 *B)
+__global__ void k_extend_yz(Lines m, int xf, int L, const double *R, double2 *B)
 {
     __shared__ double2 tile[kTile][kTile + 1];
     const int64_t l0 = (int64_t)blockIdx.x * kTile;
@@ -239,7 +293,7 @@ __global__ void k_extend_yz(Lines m, int xf, int L, const double2 *W, double2 *B
     for (int r = ty; r < kTile; r += kTileRows) {
         const int64_t line = l0 + tx;
         const int mi = m0 + r;
-        if (line < m.lines && mi < m.M) tile[r][tx] = ext_value(m, xf, L, W, line, mi);
+        if (line < m.lines && mi < m.M) tile[r][tx] = ext_value(m, xf, L, R, line, mi);
     }
     __syncthreads();
     for (int r = ty; r < kTile; r += kTileRows) {
@@ -250,7 +304,7 @@ __global__ void k_extend_yz(Lines m, int xf, int L, const double2 *W, double2 *B
 }
 
 // grid (ceil(lines / 32), ceil(L / 32)), block (32, 8)
-__global__ void k_extract_yz(Lines m, int xf, int L, const double2 *B, double2 *W)
+__global__ void k_extract_yz(Lines m, int xf, int L, const double2 *B, double *R)
 {
     __shared__ double2 tile[kTile][kTile + 1];
     const int64_t l0 = (int64_t)blockIdx.x * kTile;
@@ -265,7 +319,7 @@ __global__ void k_extract_yz(Lines m, int xf, int L, const double2 *B, double2 *
     for (int r = ty; r < kTile; r += kTileRows) {
         const int64_t line = l0 + tx;
         const int k = k0 + r;
-        if (line < m.lines && k < L) W[w_index(m, line, k)] = tile[tx][r];
+        if (line < m.lines && k < L) store_pair(m, R, line, k, tile[tx][r]);
     }
 }
 
@@ -286,8 +340,8 @@ __device__ __forceinline__ int64_t block_index(const Block &b, int i, int j, int
     return i + (int64_t)(b.n[0] + 1) * (j + (int64_t)(b.n[1] + 1) * k);
 }
 
-// phi = rho + wall terms on the logical range, as complex values.
-__global__ void k_pack(Block b, const double *rho, double2 *W)
+// phi = rho + wall terms on the logical range.
+__global__ void k_pack(Block b, const double *rho, double *R)
 {
     const int64_t total = (int64_t)b.L[0] * b.L[1] * b.L[2];
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
@@ -301,12 +355,12 @@ __global__ void k_pack(Block b, const double *rho, double2 *W)
             if (g[d] == b.term_node_lo[d]) v += b.term_lo[d];
             if (g[d] == b.term_node_hi[d]) v += b.term_hi[d];
         }
-        W[t] = make_double2(v, 0.0);
+        R[t] = v;
     }
 }
 
 // Division by the table (sum of three per-axis terms, added x, y, then z).
-__global__ void k_divide(Block b, const double *tx, const double *ty, const double *tz, double2 *W)
+__global__ void k_divide(Block b, const double *tx, const double *ty, const double *tz, double *R)
 {
     const int64_t total = (int64_t)b.L[0] * b.L[1] * b.L[2];
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
@@ -314,20 +368,13 @@ __global__ void k_divide(Block b, const double *tx, const double *ty, const doub
         const int j = (int)((t / b.L[0]) % b.L[1]);
         const int k = (int)(t / ((int64_t)b.L[0] * b.L[1]));
         const double den = (tx[i] + ty[j]) + tz[k];
-        double2 v = W[t];
-        if (den == 0.0 || (b.zero_first && t == 0)) {
-            v = make_double2(0.0, 0.0);
-        } else {
-            v.x = v.x / den;
-            v.y = v.y / den;
-        }
-        W[t] = v;
+        R[t] = den == 0.0 || (b.zero_first && t == 0) ? 0.0 : R[t] / den;
     }
 }
 
 // phi on every block node: the transform's nodes scaled by the normalisers, a
 // periodic axis' node n as the image of node 0, a Dirichlet wall its value.
-__global__ void k_unpack(Block b, const double2 *W, double *phi)
+__global__ void k_unpack(Block b, const double *R, double *phi)
 {
     const int B0 = b.n[0] + 1, B1 = b.n[1] + 1;
     const int64_t total = (int64_t)B0 * B1 * (b.n[2] + 1);
@@ -348,7 +395,7 @@ __global__ void k_unpack(Block b, const double2 *W, double *phi)
         }
         if (!wall) {
             const int64_t at = (g[0] - b.ls[0]) + (int64_t)b.L[0] * ((g[1] - b.ls[1]) + (int64_t)b.L[1] * (g[2] - b.ls[2]));
-            v = W[at].x / b.norm;
+            v = R[at] / b.norm;
         }
         phi[t] = v;
     }
@@ -409,7 +456,8 @@ struct ohpic_poisson {
     Lines lines[3];
     cufftHandle plan[3] = {0, 0, 0};
     bool planned[3] = {false, false, false};
-    double2 *W = nullptr, *B = nullptr;
+    double *R = nullptr;
+    double2 *B = nullptr;
     double *table[3] = {nullptr, nullptr, nullptr};
     double *rho = nullptr, *phi = nullptr, *e = nullptr;   // device staging of the host entry point
     cudaStream_t stream = nullptr;
@@ -433,32 +481,32 @@ void release(ohpic_poisson *p)
         if (p->planned[d]) cufftDestroy(p->plan[d]);
         if (p->table[d]) cudaFree(p->table[d]);
     }
-    for (void *q : {(void *)p->W, (void *)p->B, (void *)p->rho, (void *)p->phi, (void *)p->e})
+    for (void *q : {(void *)p->R, (void *)p->B, (void *)p->rho, (void *)p->phi, (void *)p->e})
         if (q) cudaFree(q);
     if (p->stream) cudaStreamDestroy(p->stream);
 }
 
-// forward or backward transform along one axis of p->W
+// forward or backward transform along one axis of p->R
 int transform(ohpic_poisson *p, int d, int xf, cudaStream_t st)
 {
     const Lines &m = p->lines[d];
     const int L = p->ax[d].L;
     const unsigned lt = (unsigned)((m.lines + kTile - 1) / kTile);
     if (d == 0)
-        k_extend_x<<<grid_of((int64_t)m.M * m.lines), 256, 0, st>>>(m, xf, L, p->W, p->B);
+        k_extend_x<<<grid_of((int64_t)m.M * m.lines), 256, 0, st>>>(m, xf, L, p->R, p->B);
     else
-        k_extend_yz<<<dim3(lt, (unsigned)((m.M + kTile - 1) / kTile)), dim3(kTile, kTileRows), 0, st>>>(m, xf, L, p->W,
+        k_extend_yz<<<dim3(lt, (unsigned)((m.M + kTile - 1) / kTile)), dim3(kTile, kTileRows), 0, st>>>(m, xf, L, p->R,
                                                                                                       p->B);
     if (cufftSetStream(p->plan[d], st) != CUFFT_SUCCESS)
         return pfail(p, OHPIC_ERR_CUDA, "cufftSetStream failed");
-    const int dir = xf == XF_IDFT ? CUFFT_INVERSE : CUFFT_FORWARD;
+    const int dir = xf == XF_HC2R ? CUFFT_INVERSE : CUFFT_FORWARD;
     const cufftResult r = cufftExecZ2Z(p->plan[d], (cufftDoubleComplex *)p->B, (cufftDoubleComplex *)p->B, dir);
     if (r != CUFFT_SUCCESS) return pfail(p, OHPIC_ERR_CUDA, "cufftExecZ2Z failed (" + std::to_string((int)r) + ")");
     if (d == 0)
-        k_extract_x<<<grid_of((int64_t)L * m.lines), 256, 0, st>>>(m, xf, L, p->B, p->W);
+        k_extract_x<<<grid_of((int64_t)L * m.lines), 256, 0, st>>>(m, xf, L, p->B, p->R);
     else
         k_extract_yz<<<dim3(lt, (unsigned)((L + kTile - 1) / kTile)), dim3(kTile, kTileRows), 0, st>>>(m, xf, L, p->B,
-                                                                                                     p->W);
+                                                                                                     p->R);
     return OHPIC_OK;
 }
 
@@ -539,18 +587,30 @@ int ohpic_poisson_create(const int32_t n[3], const int32_t kinds[3], const doubl
     const int64_t nl = (int64_t)b.L[0] * b.L[1] * b.L[2];
     int64_t maxb = 0;
     for (int d = 0; d < 3; ++d) {
+        // pair along the longer of the two other axes (the slower one on a tie)
         Lines &m = p->lines[d];
+        const int u = d == 0 ? 1 : 0, v = d == 2 ? 1 : 2;
+        const int pk = b.L[u] > b.L[v] ? u : v;
+        const int H = (b.L[pk] + 1) / 2;
+        int P[3] = {b.L[0], b.L[1], b.L[2]};
+        P[pk] = H;
         m.axis = d;
+        m.pack = pk;
+        m.P0 = P[0];
+        m.P1 = P[1];
+        m.P2 = P[2];
         m.L0 = b.L[0];
         m.L1 = b.L[1];
-        m.L2 = b.L[2];
-        m.lines = nl / b.L[d];
+        m.H = H;
+        m.Lp = b.L[pk];
+        m.pstride = (int64_t)H * (pk == 0 ? 1 : (pk == 1 ? (int64_t)b.L[0] : (int64_t)b.L[0] * b.L[1]));
+        m.lines = (int64_t)P[0] * P[1] * P[2] / P[d];
         m.M = p->ax[d].M;
         maxb = std::max<int64_t>(maxb, (int64_t)m.M * m.lines);
     }
     int rc = OHPIC_OK;
     if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) rc = OHPIC_ERR_CUDA;
-    if (rc == OHPIC_OK && (cudaMalloc((void **)&p->W, sizeof(double2) * nl) != cudaSuccess ||
+    if (rc == OHPIC_OK && (cudaMalloc((void **)&p->R, sizeof(double) * nl) != cudaSuccess ||
                            cudaMalloc((void **)&p->B, sizeof(double2) * maxb) != cudaSuccess))
         rc = pfail(p, OHPIC_ERR_OOM, "poisson: device buffers");
     for (int d = 0; d < 3 && rc == OHPIC_OK; ++d) {
@@ -605,17 +665,17 @@ int ohpic_poisson_solve_device(ohpic_poisson *p, const double *rho, double *phi,
     cudaStream_t st = (cudaStream_t)stream;
     const Block &b = p->blk;
     const int64_t nl = (int64_t)b.L[0] * b.L[1] * b.L[2];
-    k_pack<<<grid_of(nl), 256, 0, st>>>(b, rho, p->W);
+    k_pack<<<grid_of(nl), 256, 0, st>>>(b, rho, p->R);
     for (int d = 0; d < 3; ++d) {
         const int rc = transform(p, d, p->ax[d].fwd, st);
         if (rc != OHPIC_OK) return rc;
     }
-    k_divide<<<grid_of(nl), 256, 0, st>>>(b, p->table[0], p->table[1], p->table[2], p->W);
+    k_divide<<<grid_of(nl), 256, 0, st>>>(b, p->table[0], p->table[1], p->table[2], p->R);
     for (int d = 2; d >= 0; --d) {
         const int rc = transform(p, d, p->ax[d].bwd, st);
         if (rc != OHPIC_OK) return rc;
     }
-    k_unpack<<<grid_of(p->nodes), 256, 0, st>>>(b, p->W, phi);
+    k_unpack<<<grid_of(p->nodes), 256, 0, st>>>(b, p->R, phi);
     if (e) k_efield<<<grid_of(p->nodes), 256, 0, st>>>(b, phi, e);
     const cudaError_t ce = cudaGetLastError();
     if (ce != cudaSuccess) return pfail(p, OHPIC_ERR_CUDA, std::string("poisson: ") + cudaGetErrorString(ce));
