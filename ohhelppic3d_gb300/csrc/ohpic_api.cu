@@ -80,7 +80,8 @@ void species_consts(const ohpic_config &cfg, int s, double dt, SpeciesConst &k)
     const double tt = k.t[0] * k.t[0] + k.t[1] * k.t[1] + k.t[2] * k.t[2];
     for (int d = 0; d < 3; ++d) k.s[d] = 2.0 * k.t[d] / (1.0 + tt);
     k.mass = k.q / k.qm;
-    k.hq32 = (float)(k.qm * k.dt2);
+    k.hq = k.qm * k.dt2;
+    k.hq32 = (float)k.hq;
     k.dt32 = (float)dt;
     for (int d = 0; d < 3; ++d) {
         k.t32[d] = (float)k.t[d];

@@ -72,6 +72,7 @@ struct SpeciesConst {
     double t[3];           // qm*B*dt2 (:42)
     double s[3];           // 2t/(1+|t|^2) (:43)
     double mass;           // q/qm
+    double hq;             // qm*dt2 rounded once: the plain FP64 push's half kick is one FMA per component
     // The FP32 push's constants, rounded once on the host from the values
     // above: qm*dt2, dt, t, s.  Read as floats, the kernel never converts (a
     // conversion from double runs on GB300's narrow FP64 pipe).

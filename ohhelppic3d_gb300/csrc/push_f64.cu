@@ -335,19 +335,36 @@ __global__ void __launch_bounds__(256, 2) tiled_f64(TileArgs a, PartF64 p)
                 }
                 if (kMove) {
                     // Boris (particle_mover_boris.f90:42-56); t and s are per-species constants.
-                    const double qm = c.qm, dt2 = c.dt2;
-                    const double upm0 = Ops::add(VX[j], Ops::mul(Ops::mul(qm, ex), dt2));
-                    const double upm1 = Ops::add(VY[j], Ops::mul(Ops::mul(qm, ey), dt2));
-                    const double upm2 = Ops::add(VZ[j], Ops::mul(Ops::mul(qm, ez), dt2));
+                    // Strict: the half kick (qm*E)*dt2 in the reference's order.  Otherwise
+                    // hq = qm*dt2 is rounded once on the host and each half kick is one
+                    // FMA (six FP64 operations fewer per particle on the narrow FP64 pipe).
+                    double upm0, upm1, upm2;
+                    if (STRICT) {
+                        const double qm = c.qm, dt2 = c.dt2;
+                        upm0 = Ops::add(VX[j], Ops::mul(Ops::mul(qm, ex), dt2));
+                        upm1 = Ops::add(VY[j], Ops::mul(Ops::mul(qm, ey), dt2));
+                        upm2 = Ops::add(VZ[j], Ops::mul(Ops::mul(qm, ez), dt2));
+                    } else {
+                        upm0 = fma(c.hq, ex, VX[j]);
+                        upm1 = fma(c.hq, ey, VY[j]);
+                        upm2 = fma(c.hq, ez, VZ[j]);
+                    }
                     const double upa0 = Ops::add(upm0, Ops::sub(Ops::mul(upm1, c.t[2]), Ops::mul(upm2, c.t[1])));
                     const double upa1 = Ops::add(upm1, Ops::sub(Ops::mul(upm2, c.t[0]), Ops::mul(upm0, c.t[2])));
                     const double upa2 = Ops::add(upm2, Ops::sub(Ops::mul(upm0, c.t[1]), Ops::mul(upm1, c.t[0])));
                     const double upp0 = Ops::add(upm0, Ops::sub(Ops::mul(upa1, c.s[2]), Ops::mul(upa2, c.s[1])));
                     const double upp1 = Ops::add(upm1, Ops::sub(Ops::mul(upa2, c.s[0]), Ops::mul(upa0, c.s[2])));
                     const double upp2 = Ops::add(upm2, Ops::sub(Ops::mul(upa0, c.s[1]), Ops::mul(upa1, c.s[0])));
-                    VX[j] = Ops::add(upp0, Ops::mul(Ops::mul(qm, ex), dt2));
-                    VY[j] = Ops::add(upp1, Ops::mul(Ops::mul(qm, ey), dt2));
-                    VZ[j] = Ops::add(upp2, Ops::mul(Ops::mul(qm, ez), dt2));
+                    if (STRICT) {
+                        const double qm = c.qm, dt2 = c.dt2;
+                        VX[j] = Ops::add(upp0, Ops::mul(Ops::mul(qm, ex), dt2));
+                        VY[j] = Ops::add(upp1, Ops::mul(Ops::mul(qm, ey), dt2));
+                        VZ[j] = Ops::add(upp2, Ops::mul(Ops::mul(qm, ez), dt2));
+                    } else {
+                        VX[j] = fma(c.hq, ex, upp0);
+                        VY[j] = fma(c.hq, ey, upp1);
+                        VZ[j] = fma(c.hq, ez, upp2);
+                    }
                     // Position (:60-62) and the periodic boundary applied twice; the
                     // comparisons run on the bit patterns, the rare wraps in FP64.
                     x = Ops::add(x, Ops::mul(VX[j], c.dt));
