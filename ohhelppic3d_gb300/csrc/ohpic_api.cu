@@ -332,7 +332,7 @@ int ohpic_destroy(ohpic_ctx *c)
         dfree(c->pblock[b]);   // holds the particle arrays and the ids
     }
     dfree(c->rho); dfree(c->phi); dfree(c->epad); dfree(c->spec); dfree(c->green); dfree(c->wsum);
-    dfree(c->cell_count); dfree(c->cell_start); dfree(c->scan_tmp); dfree(c->key_table); dfree(c->tile_begin);
+    dfree(c->cell_count); dfree(c->cell_stay); dfree(c->cell_start); dfree(c->scan_tmp); dfree(c->key_table); dfree(c->tile_begin);
     dfree(c->stage); dfree(c->interp_buf); dfree(c->diag);
     if (c->diag_host) cudaFreeHost(c->diag_host);
     fields_teardown(c);
@@ -428,6 +428,7 @@ int ohpic_create(const ohpic_config *cfg, ohpic_ctx **out)
     if (rc == OHPIC_OK) rc = dalloc(c, (char **)&c->spec, g.nspec * 2 * es);
     if (rc == OHPIC_OK) rc = dalloc(c, &c->green, g.nspec);
     if (rc == OHPIC_OK) rc = dalloc(c, &c->cell_count, g.ncell);
+    if (rc == OHPIC_OK) rc = dalloc(c, &c->cell_stay, g.ncell);
     if (rc == OHPIC_OK) rc = dalloc(c, &c->cell_start, g.ncell + 1);
     if (rc == OHPIC_OK) rc = dalloc(c, &c->scan_tmp, scan_tmp_elems(g.ncell));
     if (rc == OHPIC_OK) rc = dalloc(c, &c->key_table, (int64_t)g.nx + g.ny + g.nz);

@@ -240,6 +240,7 @@ struct ohpic_ctx {
 
     // sort
     uint32_t *cell_count;   // ncell
+    uint32_t *cell_stay;    // ncell: the tile-local re-sort's stayer counts
     uint32_t *cell_start;   // ncell + 1
     uint32_t *scan_tmp;
     uint32_t *key_table;    // nx + ny + nz per-axis terms of the tile-major key

@@ -32,7 +32,7 @@
 // record in the second buffer; the next push (tiled_f32_rec) reads those
 // records in place of the seven arrays and writes the arrays and the ids, so
 // the sort has no transpose pass of its own.  The arithmetic is the same
-// advance(), so both pushes give the same bits.
+// advance_pair(), so both pushes give the same bits.
 #include <type_traits>
 
 #include "tile_common.cuh"
@@ -135,28 +135,64 @@ __device__ __forceinline__ void warp_run_deposit(int key, unsigned u[8], unsigne
     if (head && key >= 0) box_add8(hi, lo, key, sx, sxy, u);
 }
 
+// Componentwise FP32 pair arithmetic.  GB300 issues each of these as one
+// instruction for both components, and each component is rounded exactly as the
+// scalar operation (__fmul_rn, __fadd_rn, __fmaf_rn): no contraction.  The push
+// carries two particles through one instruction stream this way, so every
+// particle's arithmetic is the same sequence of roundings whichever pair or lane
+// it sits in.
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 bc2(float v) { return make_float2(v, v); }
+// 1 - r, rounded once (r * -1 is exact).
+__device__ __forceinline__ float2 one_minus2(float2 r) { return __ffma2_rn(r, bc2(-1.f), bc2(1.f)); }
+
+// CIC weights of nodes floor(x) and floor(x)+1 for a pair of offsets.
+template <int CONV>
+__device__ __forceinline__ void cic2(float2 r, float2 &w0, float2 &w1)
+{
+    if (CONV == OHPIC_WEIGHTS_REFERENCE) {
+        w0 = r;
+        w1 = one_minus2(r);
+    } else {
+        w0 = one_minus2(r);
+        w1 = r;
+    }
+}
+
 // CIC weights of one particle in units of 2^-24, summing to exactly 2^24.  The
 // total is split exactly, one axis at a time: x into X1 = round(wx1 * 2^24) and
 // X0 = 2^24 - X1, each half into y parts, each quarter into z parts.  A child is
 // rounded from its parent's FP32 product and clamped to the parent's integer, the
 // sibling is the difference, so every weight is non-negative and the eight add
 // up to 2^24 with no fix-up pass (7 float-to-integer conversions instead of 8).
-template <int W>
-__device__ __forceinline__ void fixed_weights(float ox, float oy, float oz, unsigned u[8])
+// The products come in for a pair of particles (component c of each argument).
+__device__ __forceinline__ void split_weights(float fx1, float f11, float f01, float z00, float z10, float z01,
+                                              float z11, unsigned u[8])
 {
-    float wx0, wx1, wy0, wy1, wz0, wz1;
-    cic_c<W, float>(ox, wx0, wx1);
-    cic_c<W, float>(oy, wy0, wy1);
-    cic_c<W, float>(oz, wz0, wz1);
-    const float fx1 = wx1 * kWeightScale, fx0 = wx0 * kWeightScale;   // exact: power-of-two scale
     const unsigned X1 = __float2uint_rn(fx1), X0 = (1u << 24) - X1;
-    const float f11 = fx1 * wy1, f01 = fx0 * wy1, f10 = fx1 * wy0, f00 = fx0 * wy0;
     const unsigned Y11 = min(__float2uint_rn(f11), X1), Y01 = min(__float2uint_rn(f01), X0);
     const unsigned Y10 = X1 - Y11, Y00 = X0 - Y01;
-    const unsigned Z00 = min(__float2uint_rn(f00 * wz1), Y00), Z10 = min(__float2uint_rn(f10 * wz1), Y10);
-    const unsigned Z01 = min(__float2uint_rn(f01 * wz1), Y01), Z11 = min(__float2uint_rn(f11 * wz1), Y11);
+    const unsigned Z00 = min(__float2uint_rn(z00), Y00), Z10 = min(__float2uint_rn(z10), Y10);
+    const unsigned Z01 = min(__float2uint_rn(z01), Y01), Z11 = min(__float2uint_rn(z11), Y11);
     u[0] = Y00 - Z00; u[1] = Y10 - Z10; u[2] = Y01 - Z01; u[3] = Y11 - Z11;
     u[4] = Z00; u[5] = Z10; u[6] = Z01; u[7] = Z11;
+}
+
+template <int W>
+__device__ __forceinline__ void fixed_weights2(float2 ox, float2 oy, float2 oz, unsigned u0[8], unsigned u1[8])
+{
+    float2 wx0, wx1, wy0, wy1, wz0, wz1;
+    cic2<W>(ox, wx0, wx1);
+    cic2<W>(oy, wy0, wy1);
+    cic2<W>(oz, wz0, wz1);
+    const float2 S = bc2(kWeightScale);
+    const float2 fx1 = mul2(wx1, S), fx0 = mul2(wx0, S);   // exact: power-of-two scale
+    const float2 f11 = mul2(fx1, wy1), f01 = mul2(fx0, wy1), f10 = mul2(fx1, wy0), f00 = mul2(fx0, wy0);
+    const float2 z00 = mul2(f00, wz1), z10 = mul2(f10, wz1), z01 = mul2(f01, wz1), z11 = mul2(f11, wz1);
+    split_weights(fx1.x, f11.x, f01.x, z00.x, z10.x, z01.x, z11.x, u0);
+    split_weights(fx1.y, f11.y, f01.y, z00.y, z10.y, z01.y, z11.y, u1);
 }
 
 __device__ __forceinline__ void deposit_global_fixed(const Geom &g, unsigned long long *w, int ix, int iy, int iz,
@@ -416,14 +452,51 @@ struct Tally {
     float ke = 0.f, px = 0.f, py = 0.f, pz = 0.f;
 };
 
-// One particle: gather (MODE != DEPOSIT), Boris + offset update + periodic cell
-// wrap (PUSH/MOVE), interp output (INTERP) and the fixed-point CIC weights of
-// the (new) position (PUSH/DEPOSIT).  Returns the box index of the deposit cell,
-// or -1 when there is no shared deposit (no deposit mode, outside the box: then
-// the weights already went to global memory, or an invalid cell).
+// One particle's E at its 8 nodes (staged box when key >= 0, else global
+// memory), interpolated with component C of the pair weights ww.
+template <int C>
+__device__ __forceinline__ float3 gather1(const TileArgs &a, const Box &box, int key, int ix, int iy, int iz,
+                                          const float4 *sE, const float2 ww[8])
+{
+    float4 nd[8];
+    load_nodes<float4>(a, box, key, ix, iy, iz, sE, nd);
+    float ex = 0.f, ey = 0.f, ez = 0.f;
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+        const float w = C == 0 ? ww[n].x : ww[n].y;
+        ex = fmaf(nd[n].x, w, ex);
+        ey = fmaf(nd[n].y, w, ey);
+        ez = fmaf(nd[n].z, w, ez);
+    }
+    return make_float3(ex, ey, ez);
+}
+
+// Offset o in cell units after the move: the integer part goes to the cell
+// index, o keeps the fraction in [0, 1).  o - floor(o) rounds to 1 for a tiny
+// negative o, which is the next cell's 0.
+__device__ __forceinline__ void carry(float &o, float f, int &i)
+{
+    if (o >= 1.f) {
+        o = 0.f;
+        f += 1.f;
+    }
+    i += (int)f;
+}
+
+// Two particles s0, s1 (v0, v1: slot inside the species' count): gather (MODE !=
+// DEPOSIT), Boris + offset update + periodic cell wrap (PUSH/MOVE), interp output
+// (INTERP) and the fixed-point CIC weights of the (new) position (PUSH/DEPOSIT).
+// Each particle's arithmetic is the scalar sequence the reference writes
+// (particle_mover_boris.f90:42-62, linear_interpolator.f90:54-66), carried for
+// both particles by the pair instructions above.  dk[p] is the box index of
+// particle p's deposit cell, or -1 when it has no shared deposit (no deposit
+// mode, a slot past the count, or outside the box: then its weights already went
+// to global memory).  A slot past the count is computed on a stand-in cell in
+// the box and neither deposits, counts nor writes interp output.
 template <int MODE, int W>
-__device__ __forceinline__ int advance(const TileArgs &a, const Box &box, bool e_ok, const float4 *sE, int sp,
-                                       const Push32 &k, int64_t idx, P32 &s, unsigned u[8], Tally &t)
+__device__ __forceinline__ void advance_pair(const TileArgs &a, const Box &box, bool e_ok, const float4 *sE, int sp,
+                                             const Push32 &k, int64_t idx, bool v0, bool v1, P32 &s0, P32 &s1,
+                                             unsigned u0[8], unsigned u1[8], int dk[2], Tally &t)
 {
     constexpr bool kGather = MODE != MODE_DEPOSIT;
     constexpr bool kMove = MODE == MODE_PUSH || MODE == MODE_MOVE;
@@ -433,69 +506,112 @@ __device__ __forceinline__ int advance(const TileArgs &a, const Box &box, bool e
     // into the grid (flagging anything else), the push wraps every cell it
     // writes, and a restored snapshot is checked on load.  So no per-particle
     // range check here (it cost 2.5% of the push).
-    int ix = cell_x(s.cell), iy = cell_y(s.cell), iz = cell_z(s.cell);
+    const int32_t standin = pack_cell(box.ox + g.halo, box.oy + g.halo, box.oz + g.halo);
+    if (!v0) s0.cell = standin;
+    if (!v1) s1.cell = standin;
+    int ix0 = cell_x(s0.cell), iy0 = cell_y(s0.cell), iz0 = cell_z(s0.cell);
+    int ix1 = cell_x(s1.cell), iy1 = cell_y(s1.cell), iz1 = cell_z(s1.cell);
+    float2 ox = make_float2(s0.ox, s1.ox), oy = make_float2(s0.oy, s1.oy), oz = make_float2(s0.oz, s1.oz);
     if (kGather) {
-        const int key = box.key(ix, iy, iz);
-        t.out += key < 0;
-        float wx0, wx1, wy0, wy1, wz0, wz1;
-        cic_c<W, float>(s.ox, wx0, wx1);
-        cic_c<W, float>(s.oy, wy0, wy1);
-        cic_c<W, float>(s.oz, wz0, wz1);
-        const float a00 = wx0 * wy0, a10 = wx1 * wy0, a01 = wx0 * wy1, a11 = wx1 * wy1;
-        const float ww[8] = {a00 * wz0, a10 * wz0, a01 * wz0, a11 * wz0, a00 * wz1, a10 * wz1, a01 * wz1, a11 * wz1};
-        float4 nd[8];
-        load_nodes<float4>(a, box, e_ok ? key : -1, ix, iy, iz, sE, nd);
-        float ex = 0.f, ey = 0.f, ez = 0.f;
-#pragma unroll
-        for (int n = 0; n < 8; ++n) {
-            ex = fmaf(nd[n].x, ww[n], ex);
-            ey = fmaf(nd[n].y, ww[n], ey);
-            ez = fmaf(nd[n].z, ww[n], ez);
-        }
+        const int key0 = box.key(ix0, iy0, iz0), key1 = box.key(ix1, iy1, iz1);
+        t.out += (unsigned)(v0 && key0 < 0) + (unsigned)(v1 && key1 < 0);
+        float2 wx0, wx1, wy0, wy1, wz0, wz1;
+        cic2<W>(ox, wx0, wx1);
+        cic2<W>(oy, wy0, wy1);
+        cic2<W>(oz, wz0, wz1);
+        const float2 a00 = mul2(wx0, wy0), a10 = mul2(wx1, wy0), a01 = mul2(wx0, wy1), a11 = mul2(wx1, wy1);
+        const float2 ww[8] = {mul2(a00, wz0), mul2(a10, wz0), mul2(a01, wz0), mul2(a11, wz0),
+                              mul2(a00, wz1), mul2(a10, wz1), mul2(a01, wz1), mul2(a11, wz1)};
+        const float3 e0 = gather1<0>(a, box, e_ok ? key0 : -1, ix0, iy0, iz0, sE, ww);
+        const float3 e1 = gather1<1>(a, box, e_ok ? key1 : -1, ix1, iy1, iz1, sE, ww);
         if (MODE == MODE_INTERP) {
             double *o = a.interp_out + 3 * idx;
-            o[0] = ex;
-            o[1] = ey;
-            o[2] = ez;
+            if (v0) { o[0] = e0.x; o[1] = e0.y; o[2] = e0.z; }
+            if (v1) { o[3] = e1.x; o[4] = e1.y; o[5] = e1.z; }
         }
         if (kMove) {
-            // Boris rotation with per-species t and s (particle_mover_boris.f90:42-56).
-            const float hx = k.hq * ex, hy = k.hq * ey, hz = k.hq * ez;
-            const float um0 = s.vx + hx, um1 = s.vy + hy, um2 = s.vz + hz;
-            const float ua0 = um0 + (um1 * k.t2 - um2 * k.t1);
-            const float ua1 = um1 + (um2 * k.t0 - um0 * k.t2);
-            const float ua2 = um2 + (um0 * k.t1 - um1 * k.t0);
-            s.vx = um0 + (ua1 * k.s2 - ua2 * k.s1) + hx;
-            s.vy = um1 + (ua2 * k.s0 - ua0 * k.s2) + hy;
-            s.vz = um2 + (ua0 * k.s1 - ua1 * k.s0) + hz;
-            // Offset update in cell units; a crossing moves the integer cell
-            // (wrapped periodically) and keeps the offset in [0, 1).
-            float nxo = fmaf(s.vx, k.dt, s.ox), nyo = fmaf(s.vy, k.dt, s.oy), nzo = fmaf(s.vz, k.dt, s.oz);
-            float fx = floorf(nxo), fy = floorf(nyo), fz = floorf(nzo);
-            nxo -= fx; nyo -= fy; nzo -= fz;
-            if (nxo >= 1.f) { nxo = 0.f; fx += 1.f; }
-            if (nyo >= 1.f) { nyo = 0.f; fy += 1.f; }
-            if (nzo >= 1.f) { nzo = 0.f; fz += 1.f; }
-            ix += (int)fx; iy += (int)fy; iz += (int)fz;
-            if ((unsigned)ix >= (unsigned)g.nx) { ++t.cx; ix = wrapi(ix, g.nx); }
-            if ((unsigned)iy >= (unsigned)g.ny) { ++t.cy; iy = wrapi(iy, g.ny); }
-            if ((unsigned)iz >= (unsigned)g.nz) { ++t.cz; iz = wrapi(iz, g.nz); }
-            s.ox = nxo; s.oy = nyo; s.oz = nzo;
-            s.cell = pack_cell(ix, iy, iz);
+            // Boris rotation with per-species t and s (particle_mover_boris.f90:42-56):
+            // u- = v + h, u' = u- + u- x t, v = u- + u' x s + h with h = qm dt/2 E.
+            // Each cross-product component b*c' - c*b' rounds the second product
+            // first (multiplied by the negated constant: exact) and adds it in an FMA.
+            const float2 hq = bc2(k.hq);
+            const float2 hx = mul2(hq, make_float2(e0.x, e1.x));
+            const float2 hy = mul2(hq, make_float2(e0.y, e1.y));
+            const float2 hz = mul2(hq, make_float2(e0.z, e1.z));
+            const float2 um0 = add2(make_float2(s0.vx, s1.vx), hx);
+            const float2 um1 = add2(make_float2(s0.vy, s1.vy), hy);
+            const float2 um2 = add2(make_float2(s0.vz, s1.vz), hz);
+            const float2 ua0 = add2(um0, fma2(um1, bc2(k.t2), mul2(um2, bc2(-k.t1))));
+            const float2 ua1 = add2(um1, fma2(um2, bc2(k.t0), mul2(um0, bc2(-k.t2))));
+            const float2 ua2 = add2(um2, fma2(um0, bc2(k.t1), mul2(um1, bc2(-k.t0))));
+            const float2 vx = add2(add2(um0, fma2(ua1, bc2(k.s2), mul2(ua2, bc2(-k.s1)))), hx);
+            const float2 vy = add2(add2(um1, fma2(ua2, bc2(k.s0), mul2(ua0, bc2(-k.s2)))), hy);
+            const float2 vz = add2(add2(um2, fma2(ua0, bc2(k.s1), mul2(ua1, bc2(-k.s0)))), hz);
+            // Offset update in cell units (:60-62); a crossing moves the integer
+            // cell and keeps the offset in [0, 1).
+            ox = fma2(vx, bc2(k.dt), ox);
+            oy = fma2(vy, bc2(k.dt), oy);
+            oz = fma2(vz, bc2(k.dt), oz);
+            const float2 fx = make_float2(floorf(ox.x), floorf(ox.y));
+            const float2 fy = make_float2(floorf(oy.x), floorf(oy.y));
+            const float2 fz = make_float2(floorf(oz.x), floorf(oz.y));
+            ox = fma2(fx, bc2(-1.f), ox);
+            oy = fma2(fy, bc2(-1.f), oy);
+            oz = fma2(fz, bc2(-1.f), oz);
+            carry(ox.x, fx.x, ix0); carry(ox.y, fx.y, ix1);
+            carry(oy.x, fy.x, iy0); carry(oy.y, fy.y, iy1);
+            carry(oz.x, fz.x, iz0); carry(oz.y, fz.y, iz1);
+            // Periodic wrap of the cell (periodic_particle_boundary.f90:42-53); one
+            // branch for both particles and all axes, taken only at the box faces.
+            const bool out0 = (unsigned)ix0 >= (unsigned)g.nx || (unsigned)iy0 >= (unsigned)g.ny ||
+                              (unsigned)iz0 >= (unsigned)g.nz;
+            const bool out1 = (unsigned)ix1 >= (unsigned)g.nx || (unsigned)iy1 >= (unsigned)g.ny ||
+                              (unsigned)iz1 >= (unsigned)g.nz;
+            if (out0 || out1) {
+                if (v0) {
+                    t.cx += (unsigned)ix0 >= (unsigned)g.nx;
+                    t.cy += (unsigned)iy0 >= (unsigned)g.ny;
+                    t.cz += (unsigned)iz0 >= (unsigned)g.nz;
+                }
+                if (v1) {
+                    t.cx += (unsigned)ix1 >= (unsigned)g.nx;
+                    t.cy += (unsigned)iy1 >= (unsigned)g.ny;
+                    t.cz += (unsigned)iz1 >= (unsigned)g.nz;
+                }
+                ix0 = wrapi(ix0, g.nx); iy0 = wrapi(iy0, g.ny); iz0 = wrapi(iz0, g.nz);
+                ix1 = wrapi(ix1, g.nx); iy1 = wrapi(iy1, g.ny); iz1 = wrapi(iz1, g.nz);
+            }
+            s0.ox = ox.x; s0.oy = oy.x; s0.oz = oz.x;
+            s1.ox = ox.y; s1.oy = oy.y; s1.oz = oz.y;
+            s0.vx = vx.x; s0.vy = vy.x; s0.vz = vz.x;
+            s1.vx = vx.y; s1.vy = vy.y; s1.vz = vz.y;
+            s0.cell = pack_cell(ix0, iy0, iz0);
+            s1.cell = pack_cell(ix1, iy1, iz1);
             if (a.with_energy) {
-                t.ke = fmaf(s.vx, s.vx, fmaf(s.vy, s.vy, fmaf(s.vz, s.vz, t.ke)));
-                t.px += s.vx; t.py += s.vy; t.pz += s.vz;
+                if (v0) {
+                    t.ke = fmaf(vx.x, vx.x, fmaf(vy.x, vy.x, fmaf(vz.x, vz.x, t.ke)));
+                    t.px += vx.x; t.py += vy.x; t.pz += vz.x;
+                }
+                if (v1) {
+                    t.ke = fmaf(vx.y, vx.y, fmaf(vy.y, vy.y, fmaf(vz.y, vz.y, t.ke)));
+                    t.px += vx.y; t.py += vy.y; t.pz += vz.y;
+                }
             }
         }
     }
-    if (!kDeposit) return -1;
-    fixed_weights<W>(s.ox, s.oy, s.oz, u);
-    const int dkey = box.key(ix, iy, iz);
-    if (dkey < 0) {
-        deposit_global_fixed(g, a.wsum + (int64_t)sp * g.ncell, ix, iy, iz, u);
-        if (!kGather) ++t.out;
+    dk[0] = dk[1] = -1;
+    if (!kDeposit) return;
+    fixed_weights2<W>(ox, oy, oz, u0, u1);
+    const int d0 = box.key(ix0, iy0, iz0), d1 = box.key(ix1, iy1, iz1);
+    const bool g0 = v0 && d0 < 0, g1 = v1 && d1 < 0;
+    if (g0 || g1) {
+        unsigned long long *w = a.wsum + (int64_t)sp * g.ncell;
+        if (g0) deposit_global_fixed(g, w, ix0, iy0, iz0, u0);
+        if (g1) deposit_global_fixed(g, w, ix1, iy1, iz1, u1);
+        if (!kGather) t.out += (unsigned)g0 + (unsigned)g1;
     }
-    return dkey;
+    if (v0) dk[0] = d0;
+    if (v1) dk[1] = d1;
 }
 
 // A thread whose bounded wait for the E box gave up has gathered from global
@@ -573,8 +689,11 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
 #pragma unroll
         for (int v = 0; v < 8; ++v) u0[v] = u1[v] = 0u;
         if (gv) {
-            if (2 * gi < end) k0 = advance<MODE, W>(a, box, e_ok, sE, sp, k, 2 * gi, cur[0], u0, t);
-            if (2 * gi + 1 < end) k1 = advance<MODE, W>(a, box, e_ok, sE, sp, k, 2 * gi + 1, cur[1], u1, t);
+            int dk[2];
+            advance_pair<MODE, W>(a, box, e_ok, sE, sp, k, 2 * gi, 2 * gi < end, 2 * gi + 1 < end, cur[0], cur[1],
+                                  u0, u1, dk, t);
+            k0 = dk[0];
+            k1 = dk[1];
             if (kMove) store_pair(p, gi, cur);
         }
         if (kDeposit) {
@@ -604,7 +723,7 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
 // sums their fixed-point weights in registers while the cell stays the same,
 // adds to the shared box directly when its cell changes, and the warp combines
 // the lanes' last sums once per 128 particles.  The per-particle arithmetic is
-// advance(), as in the two-per-lane pass, and every sum is integer, so both
+// advance_pair(), as in the two-per-lane pass, and every sum is integer, so both
 // passes give the same bits.
 template <int MODE, int DEP, int W, bool REC = false>
 __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap,
@@ -682,20 +801,25 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
                 if (gi + blockDim.x < it.g1) prefetch_quad<kGather>(stage, p, gi + blockDim.x);
             }
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                if (4 * gi + j < end) {
-                    unsigned u[8];
-                    const int kk = advance<MODE, W>(a, box, e_ok, sE, sp, k, 4 * gi + j, q[j], u, t);
-                    if (kk >= 0) {
-                        if (kk != acc_key) {
-                            if (acc_key >= 0) box_add8(shi, slo, acc_key, box.sx, box.sxy, acc);
-                            acc_key = kk;
+            for (int h = 0; h < 2; ++h) {
+                const int64_t i0 = 4 * gi + 2 * h;
+                unsigned ua[8], ub[8];
+                int dk[2];
+                advance_pair<MODE, W>(a, box, e_ok, sE, sp, k, i0, i0 < end, i0 + 1 < end, q[2 * h], q[2 * h + 1],
+                                      ua, ub, dk, t);
+                // A run ends where the key changes; a particle with no shared
+                // deposit (key -1) ends it too and starts an empty one.
 #pragma unroll
-                            for (int v = 0; v < 8; ++v) acc[v] = u[v];
-                        } else {
+                for (int p2 = 0; p2 < 2; ++p2) {
+                    const unsigned *u = p2 ? ub : ua;
+                    if (dk[p2] != acc_key) {
+                        if (acc_key >= 0) box_add8(shi, slo, acc_key, box.sx, box.sxy, acc);
+                        acc_key = dk[p2];
 #pragma unroll
-                            for (int v = 0; v < 8; ++v) acc[v] += u[v];
-                        }
+                        for (int v = 0; v < 8; ++v) acc[v] = u[v];
+                    } else {
+#pragma unroll
+                        for (int v = 0; v < 8; ++v) acc[v] += u[v];
                     }
                 }
             }

@@ -290,9 +290,132 @@ __global__ void k_rec64_to_soa(const double2 *rec, int64_t seg, int64_t n, PartF
     }
 }
 
+// ---- tile-local sort: the re-sort of particles that are already tile-sorted ----
+//
+// Between two sorts a particle moves a few cells, so most of a tile's particles
+// (its source range from the last sort) still belong to that tile.  One CTA per
+// source tile counts and places those "stayers" with shared-memory counters
+// over the tile's cells; only the particles that now belong to another tile
+// ("immigrants" there) use global counters.  Each cell's range starts with its
+// stayers, then its immigrants: stay[key] is the stayer count, imm[key] the
+// immigrant count (then the immigrant cursor).  Counters are bumped once per run
+// of adjacent lanes with equal keys, and a run's lanes take consecutive slots in
+// lane order, as in the global sort.
+
+// One counter bump per run of adjacent lanes with equal keys.  The run's head
+// adds the run length to the cell's counter (shared when the cell is in this
+// CTA's tile, global otherwise); the returned value is the run's first slot
+// once tile_run_slot() has broadcast it.
+struct RunBump {
+    uint32_t base;
+    int head;   // lane of this lane's run head
+};
+
+__device__ __forceinline__ RunBump tile_run_bump(uint32_t *sh, uint32_t *gl, uint32_t key, uint32_t k0, uint32_t C,
+                                                 bool active)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t k = active ? key : 0xffffffffu - lane;   // inactive lanes end every run
+    const uint32_t prev = __shfl_up_sync(kFull, k, 1);
+    const bool head = lane == 0 || k != prev;
+    const unsigned heads = __ballot_sync(kFull, head);
+    const unsigned after = heads & ~((2u << lane) - 1u);   // run heads strictly after this lane
+    const unsigned end = after ? (unsigned)__ffs(after) - 1u : 32u;
+    RunBump r;
+    r.base = 0;
+    r.head = 31 - __clz(heads & ((2u << lane) - 1u));
+    if (active && head) {
+        const uint32_t local = key - k0;
+        r.base = local < C ? atomicAdd(sh + local, end - lane) : atomicAdd(gl + key, end - lane);
+    }
+    return r;
+}
+
+__device__ __forceinline__ uint32_t tile_run_slot(const RunBump &r)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    return __shfl_sync(kFull, r.base, r.head) + (lane - (unsigned)r.head);
+}
+
+// Counts of source tile blockIdx.x: stay[] for the tile's own cells (plain
+// stores: every cell of every tile is written), imm[] (zeroed by the caller) by
+// global atomics.
+template <bool F32>
+__global__ void __launch_bounds__(256) k_hist_tile(Geom g, const uint32_t *tab, PartF64 p64, PartF32 p32,
+                                                   const int64_t *tb, uint32_t *stay, uint32_t *imm, DevDiag *d)
+{
+    extern __shared__ uint32_t sh[];
+    constexpr int U = 4;
+    const uint32_t C = (uint32_t)g.tile_cells, k0 = (uint32_t)blockIdx.x * C;
+    for (uint32_t i = threadIdx.x; i < C; i += blockDim.x) sh[i] = 0u;
+    __syncthreads();
+    const int64_t lo = tb[blockIdx.x], hi = tb[blockIdx.x + 1];
+    for (int64_t base = lo; base < hi; base += U * (int64_t)blockDim.x) {
+        uint32_t key[U];
+        bool act[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t i = base + u * (int64_t)blockDim.x + threadIdx.x;
+            act[u] = i < hi;
+            key[u] = act[u] ? particle_key<F32>(g, tab, p64, p32, i, d) : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) tile_run_bump(sh, imm, key[u], k0, C, act[u]);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < C; i += blockDim.x) stay[k0 + i] = sh[i];
+}
+
+// Scatter of source tile blockIdx.x into whole records: a stayer at
+// start[key] + (its rank among the cell's stayers), an immigrant at
+// start[key] + stay[key] + (its rank among the cell's immigrants; imm[] zeroed
+// by the caller).  Two particles per thread per iteration, both counter bumps in
+// flight before either slot is used.
+template <bool F32>
+__global__ void __launch_bounds__(256, 4) k_scatter_tile(Geom g, const uint32_t *tab, PartF64 s64, PartF32 s32,
+                                                         const uint32_t *sid, void *rec, const int64_t *tb,
+                                                         int64_t seg, const uint32_t *start, const uint32_t *stay,
+                                                         uint32_t *imm, DevDiag *d)
+{
+    extern __shared__ uint32_t sh[];
+    constexpr int U = 2;
+    const uint32_t C = (uint32_t)g.tile_cells, k0 = (uint32_t)blockIdx.x * C;
+    for (uint32_t i = threadIdx.x; i < C; i += blockDim.x) sh[i] = 0u;
+    __syncthreads();
+    const int64_t lo = tb[blockIdx.x], hi = tb[blockIdx.x + 1];
+    for (int64_t base = lo; base < hi; base += U * (int64_t)blockDim.x) {
+        Rec<F32> r[U];
+        bool act[U];
+        uint32_t key[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t i = base + u * (int64_t)blockDim.x + threadIdx.x;
+            act[u] = i < hi;
+            if (act[u]) rec_load<F32>(s64, s32, sid, i, r[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) key[u] = act[u] ? rec_key<F32>(g, tab, r[u], d) : 0u;
+        RunBump b[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) b[u] = tile_run_bump(sh, imm, key[u], k0, C, act[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t slot = tile_run_slot(b[u]);
+            if (act[u]) {
+                const bool own = key[u] - k0 < C;
+                const int64_t j = seg + (int64_t)start[key[u]] + slot + (own ? 0u : stay[key[u]]);
+                if constexpr (F32) rec32_store((int4 *)rec, j, r[u]);
+                else rec64_store((double2 *)rec, j, r[u]);
+            }
+        }
+    }
+}
+
 // Exclusive scan of one block of kScanBlock values; block total -> sums[blockIdx].
-__global__ void __launch_bounds__(kScanThreads) k_scan_block(const uint32_t *in, uint32_t *out, int64_t n,
-                                                             uint32_t *sums)
+// in2, when given, is added to in element by element (the tile sort's stayer
+// and immigrant counts).
+__global__ void __launch_bounds__(kScanThreads) k_scan_block(const uint32_t *in, const uint32_t *in2, uint32_t *out,
+                                                             int64_t n, uint32_t *sums)
 {
     __shared__ uint32_t warp_tot[kScanThreads / 32];
     const int64_t b0 = (int64_t)blockIdx.x * kScanBlock + (int64_t)threadIdx.x * kScanItems;
@@ -301,7 +424,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_block(const uint32_t *in,
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
         const int64_t i = b0 + k;
-        v[k] = i < n ? in[i] : 0u;
+        v[k] = i < n ? in[i] + (in2 ? in2[i] : 0u) : 0u;
         local += v[k];
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -345,25 +468,27 @@ __global__ void k_tile_begin(Geom g, const uint32_t *start, int64_t seg, int64_t
     if (t == g.ntile) tb[t] = seg + count;
 }
 
-// Exclusive scan of n values (in -> out) using tmp for the block sums of every
-// level; returns the number of launches.
-int scan_levels(cudaStream_t st, const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp)
+// Exclusive scan of n values (in [+ in2] -> out) using tmp for the block sums of
+// every level; returns the number of launches.
+int scan_levels(cudaStream_t st, const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp,
+                const uint32_t *in2 = nullptr)
 {
     const int64_t nb = (n + kScanBlock - 1) / kScanBlock;
     if (nb <= 1) {
-        k_scan_block<<<1, kScanThreads, 0, st>>>(in, out, n, nullptr);
+        k_scan_block<<<1, kScanThreads, 0, st>>>(in, in2, out, n, nullptr);
         return 1;
     }
     uint32_t *sums = tmp, *sums_scan = tmp + nb;
-    k_scan_block<<<(unsigned)nb, kScanThreads, 0, st>>>(in, out, n, sums);
+    k_scan_block<<<(unsigned)nb, kScanThreads, 0, st>>>(in, in2, out, n, sums);
     const int inner = scan_levels(st, sums, sums_scan, nb, tmp + 2 * nb);
     k_add_offsets<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, n, sums_scan);
     return inner + 2;
 }
 
-void scan_exclusive(ohpic_ctx *c, const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp)
+void scan_exclusive(ohpic_ctx *c, const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp,
+                    const uint32_t *in2 = nullptr)
 {
-    c->launches += scan_levels(c->stream, in, out, n, tmp);
+    c->launches += scan_levels(c->stream, in, out, n, tmp, in2);
 }
 
 // ---- multi-run sort: every (run, species) segment in one pass per stage ----
@@ -531,6 +656,53 @@ void materialize_records(ohpic_ctx *c)
     c->rec_pending = false;
 }
 
+// Largest tile (cells) whose counters the tile-local re-sort keeps in shared memory.
+constexpr int kTileSortMaxCells = 8192;
+
+// Re-sort of particles already sorted on the current tiling (tile_begin valid):
+// per species, tile-local counts, the scan of stayers + immigrants, tile starts,
+// then the tile-local scatter into records (FP32: left for the next push; FP64:
+// transposed back here).
+static void sort_tiles(ohpic_ctx *c)
+{
+    const Geom &g = c->g;
+    const bool f32 = c->cfg.precision == OHPIC_FP32;
+    const int src = c->cur, dst = 1 - c->cur;
+    const size_t smem = sizeof(uint32_t) * (size_t)g.tile_cells;
+    for (int s = 0; s < c->cfg.nspecies; ++s) {
+        const int64_t n = c->count[s];
+        int64_t *tb = c->tile_begin + (int64_t)s * (g.ntile + 1);
+        cudaMemsetAsync(c->cell_count, 0, sizeof(uint32_t) * g.ncell, c->stream);
+        if (f32)
+            k_hist_tile<true><<<(unsigned)g.ntile, 256, smem, c->stream>>>(g, c->key_table, c->p64[src], c->p32[src],
+                                                                          tb, c->cell_stay, c->cell_count, c->diag);
+        else
+            k_hist_tile<false><<<(unsigned)g.ntile, 256, smem, c->stream>>>(g, c->key_table, c->p64[src], c->p32[src],
+                                                                           tb, c->cell_stay, c->cell_count, c->diag);
+        ++c->launches;
+        scan_exclusive(c, c->cell_stay, c->cell_start, g.ncell, c->scan_tmp, c->cell_count);
+        cudaMemsetAsync(c->cell_count, 0, sizeof(uint32_t) * g.ncell, c->stream);
+        if (f32) {
+            k_scatter_tile<true><<<(unsigned)g.ntile, 256, smem, c->stream>>>(
+                g, c->key_table, c->p64[src], c->p32[src], c->ids[src], c->pblock[dst], tb, c->seg[s], c->cell_start,
+                c->cell_stay, c->cell_count, c->diag);
+            ++c->launches;
+            c->rec_pending = true;
+        } else {
+            double2 *rec = (double2 *)c->pblock[dst];
+            k_scatter_tile<false><<<(unsigned)g.ntile, 256, smem, c->stream>>>(
+                g, c->key_table, c->p64[src], c->p32[src], c->ids[src], rec, tb, c->seg[s], c->cell_start,
+                c->cell_stay, c->cell_count, c->diag);
+            k_rec64_to_soa<<<grid_of(n), 256, 0, c->stream>>>(rec, c->seg[s], n, c->p64[src], c->ids[src]);
+            c->launches += 2;
+        }
+        // the new tile starts, after the scatter has read the old ones
+        k_tile_begin<<<(unsigned)((g.ntile + 1 + 255) / 256), 256, 0, c->stream>>>(g, c->cell_start, c->seg[s], n,
+                                                                                    tb);
+        ++c->launches;
+    }
+}
+
 int sort_particles(ohpic_ctx *c)
 {
     const Geom &g = c->g;
@@ -540,6 +712,11 @@ int sort_particles(ohpic_ctx *c)
     const int axes = g.nx + g.ny + g.nz;
     k_key_table<<<(unsigned)((axes + 255) / 256), 256, 0, c->stream>>>(g, c->key_table);
     ++c->launches;
+    if (c->sorted && g.tile_cells <= kTileSortMaxCells) {
+        sort_tiles(c);
+        c->steps_since_sort = 0;
+        return OHPIC_OK;
+    }
     for (int s = 0; s < c->cfg.nspecies; ++s) {
         const int64_t n = c->count[s];
         int64_t *tb = c->tile_begin + (int64_t)s * (g.ntile + 1);
