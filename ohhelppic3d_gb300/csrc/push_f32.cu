@@ -839,9 +839,14 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
     if (kGather) flush_diag<float>(a, sp, t.cx, t.cy, t.cz, t.out, t.ke, t.px, t.py, t.pz);
 }
 
+// The dynamic shared memory from its first 128-byte boundary (the launch
+// reserves the slack).  The offset is added to the shared array itself: a
+// round trip of the pointer through an integer hides its address space, and the
+// box loads and atomics then compile to generic instructions (18 loads and 8
+// atomics per particle in the push) instead of shared-memory ones.
 __device__ __forceinline__ unsigned char *align128(unsigned char *p)
 {
-    return (unsigned char *)(((uintptr_t)p + 127) & ~(uintptr_t)127);
+    return p + ((128u - (smem_addr(p) & 127u)) & 127u);
 }
 
 // Work item b with PPL particles per lane: 2 (every mode) or 4 (push and deposit).
