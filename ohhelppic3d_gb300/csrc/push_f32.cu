@@ -381,7 +381,7 @@ __device__ __forceinline__ void read_quad(const float4 *st, P32 r[4])
 // records back into arrays.  A quad's eight 16-byte record halves are
 // a0 b0 a1 b1 a2 b2 a3 b3 (a = cell and offsets, b = velocities and id); the
 // first seven go through the stage slots the seven arrays use, and b3 is
-// loaded into registers one quad ahead.
+// loaded into registers at the start of the quad's iteration.
 //
 // The warp stages its 32 quads together, as rows of the seven staged halves
 // (112 bytes per quad, the warp's 3.5 KB where the arrays' seven slots per
@@ -460,6 +460,24 @@ __device__ __forceinline__ float3 gather1(const TileArgs &a, const Box &box, int
 {
     float4 nd[8];
     load_nodes<float4>(a, box, key, ix, iy, iz, sE, nd);
+    float ex = 0.f, ey = 0.f, ez = 0.f;
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+        const float w = C == 0 ? ww[n].x : ww[n].y;
+        ex = fmaf(nd[n].x, w, ex);
+        ey = fmaf(nd[n].y, w, ey);
+        ez = fmaf(nd[n].z, w, ez);
+    }
+    return make_float3(ex, ey, ez);
+}
+
+// The same from the staged box alone (key >= 0).
+template <int C>
+__device__ __forceinline__ float3 gather_box(const float4 *sE, const Box &b, int key, const float2 ww[8])
+{
+    const float4 *q = sE + key;
+    const float4 nd[8] = {q[0], q[1], q[b.sx], q[b.sx + 1], q[b.sxy], q[b.sxy + 1], q[b.sxy + b.sx],
+                          q[b.sxy + b.sx + 1]};
     float ex = 0.f, ey = 0.f, ez = 0.f;
 #pragma unroll
     for (int n = 0; n < 8; ++n) {
@@ -770,10 +788,8 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
     // Prefetch stage after the boxes (16-byte aligned); the launch reserves it.
     const size_t boxes = box.on ? ((kGather ? (size_t)s3 * sizeof(float4) : 0) + (size_t)s3 * 8 + 15) & ~(size_t)15 : 0;
     float4 *stage = (float4 *)(smem + boxes);
-    int4 b3 = make_int4(0, 0, 0, 0);   // REC: the current quad's last record half
     if (REC) {
         prefetch_rec_warp(stage, rin.rec, it.g0, it.g1);
-        if (it.g0 + threadIdx.x < it.g1) b3 = __ldg(rin.rec + 8 * (it.g0 + threadIdx.x) + 7);
     } else if (it.g0 + threadIdx.x < it.g1) {
         prefetch_quad<kGather>(stage, p, it.g0 + threadIdx.x);
     }
@@ -785,28 +801,34 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
 #pragma unroll
         for (int v = 0; v < 8; ++v) acc[v] = 0u;
         P32 q[4];
-        uint4 qid;
-        int4 b3_next = make_int4(0, 0, 0, 0);
         if (REC) {
+            // The quad's last record half, loaded here and first used by the
+            // second pair: its 32-byte sector came into L2 with the staged copy of
+            // the same quad's a3 half, one iteration ago.
+            const int4 b3 = gi < it.g1 ? __ldg(rin.rec + 8 * gi + 7) : make_int4(0, 0, 0, 0);
+            uint4 qid;
             // the whole warp: its lanes read each other's copies, and the next
             // copies overwrite the stage only after every lane has read it
             read_rec(stage, b3, q, qid);
             __syncwarp();
             if (base + blockDim.x < it.g1) prefetch_rec_warp(stage, rin.rec, base + blockDim.x, it.g1);
-            if (gi + blockDim.x < it.g1) b3_next = __ldg(rin.rec + 8 * (gi + blockDim.x) + 7);
+            // the ids go out at once, so they hold no registers through the quad
+            if (rin.ids && gi < it.g1) *(uint4 *)(rin.ids + 4 * gi) = qid;
         }
         if (gi < it.g1) {
             if (!REC) {
                 read_quad<kGather>(stage, q);
                 if (gi + blockDim.x < it.g1) prefetch_quad<kGather>(stage, p, gi + blockDim.x);
             }
+            // particles of the quad inside the species' count (4 but at its end)
+            const int nv = (int)min(end - 4 * gi, (int64_t)4);
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const int64_t i0 = 4 * gi + 2 * h;
                 unsigned ua[8], ub[8];
                 int dk[2];
-                advance_pair<MODE, W>(a, box, e_ok, sE, sp, k, i0, i0 < end, i0 + 1 < end, q[2 * h], q[2 * h + 1],
-                                      ua, ub, dk, t);
+                advance_pair<MODE, W>(a, box, e_ok, sE, sp, k, i0, 2 * h < nv, 2 * h + 1 < nv, q[2 * h],
+                                      q[2 * h + 1], ua, ub, dk, t);
                 // A run ends where the key changes; a particle with no shared
                 // deposit (key -1) ends it too and starts an empty one.
 #pragma unroll
@@ -824,10 +846,6 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
                 }
             }
             if (kMove) store_quad(p, gi, q);
-            if (REC) {
-                if (rin.ids) *(uint4 *)(rin.ids + 4 * gi) = qid;
-                b3 = b3_next;
-            }
         }
         warp_run_deposit<DEP>(acc_key, acc, slo, shi, box.sx, box.sxy);
     }

@@ -337,6 +337,38 @@ __device__ __forceinline__ uint32_t tile_run_slot(const RunBump &r)
     return __shfl_sync(kFull, r.base, r.head) + (lane - (unsigned)r.head);
 }
 
+// The per-axis key table in shared memory: each CTA of a tile kernel copies it
+// once, and every particle's three lookups are then shared loads instead of
+// dependent global ones.
+__device__ __forceinline__ uint32_t *stage_key_table(const Geom &g, const uint32_t *tab, uint32_t *dst)
+{
+    const int nt = g.nx + g.ny + g.nz;
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) dst[i] = __ldg(tab + i);
+    return dst;
+}
+
+__device__ __forceinline__ uint32_t shared_key(const Geom &g, const uint32_t *stab, int32_t c, DevDiag *d)
+{
+    int ix = cell_x(c), iy = cell_y(c), iz = cell_z(c);
+    if ((unsigned)ix >= (unsigned)g.nx || (unsigned)iy >= (unsigned)g.ny || (unsigned)iz >= (unsigned)g.nz) {
+        if (atomicCAS(&d->err_code, 0, OHPIC_ERR_BOUNDS) == 0) d->err_info = 11;
+        ix = iy = iz = 0;
+    }
+    return stab[ix] + stab[g.nx + iy] + stab[g.nx + g.ny + iz];
+}
+
+template <bool F32>
+__device__ __forceinline__ uint32_t shared_key_xyz(const Geom &g, const uint32_t *stab, double x, double y,
+                                                   double z, DevDiag *d)
+{
+    int ix = (int)x, iy = (int)y, iz = (int)z;
+    if ((unsigned)ix >= (unsigned)g.nx || (unsigned)iy >= (unsigned)g.ny || (unsigned)iz >= (unsigned)g.nz) {
+        if (atomicCAS(&d->err_code, 0, OHPIC_ERR_BOUNDS) == 0) d->err_info = 11;
+        ix = iy = iz = 0;
+    }
+    return stab[ix] + stab[g.nx + iy] + stab[g.nx + g.ny + iz];
+}
+
 // Counts of source tile blockIdx.x: stay[] for the tile's own cells (plain
 // stores: every cell of every tile is written), imm[] (zeroed by the caller) by
 // global atomics.
@@ -345,19 +377,37 @@ __global__ void __launch_bounds__(256) k_hist_tile(Geom g, const uint32_t *tab, 
                                                    const int64_t *tb, uint32_t *stay, uint32_t *imm, DevDiag *d)
 {
     extern __shared__ uint32_t sh[];
-    constexpr int U = 4;
+    constexpr int U = F32 ? 8 : 4;
     const uint32_t C = (uint32_t)g.tile_cells, k0 = (uint32_t)blockIdx.x * C;
     for (uint32_t i = threadIdx.x; i < C; i += blockDim.x) sh[i] = 0u;
+    const uint32_t *stab = stage_key_table(g, tab, sh + C);
     __syncthreads();
     const int64_t lo = tb[blockIdx.x], hi = tb[blockIdx.x + 1];
     for (int64_t base = lo; base < hi; base += U * (int64_t)blockDim.x) {
         uint32_t key[U];
         bool act[U];
+        if constexpr (F32) {
+            int32_t cell[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int64_t i = base + u * (int64_t)blockDim.x + threadIdx.x;
-            act[u] = i < hi;
-            key[u] = act[u] ? particle_key<F32>(g, tab, p64, p32, i, d) : 0u;
+            for (int u = 0; u < U; ++u) {   // every load of the iteration first
+                const int64_t i = base + u * (int64_t)blockDim.x + threadIdx.x;
+                act[u] = i < hi;
+                cell[u] = act[u] ? p32.cell[i] : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) key[u] = act[u] ? shared_key(g, stab, cell[u], d) : 0u;
+        } else {
+            double px[U], py[U], pz[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int64_t i = base + u * (int64_t)blockDim.x + threadIdx.x;
+                act[u] = i < hi;
+                px[u] = act[u] ? p64.x[i] : 0.0;
+                py[u] = act[u] ? p64.y[i] : 0.0;
+                pz[u] = act[u] ? p64.z[i] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) key[u] = act[u] ? shared_key_xyz<F32>(g, stab, px[u], py[u], pz[u], d) : 0u;
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) tile_run_bump(sh, imm, key[u], k0, C, act[u]);
@@ -381,6 +431,7 @@ __global__ void __launch_bounds__(256, 4) k_scatter_tile(Geom g, const uint32_t 
     constexpr int U = 2;
     const uint32_t C = (uint32_t)g.tile_cells, k0 = (uint32_t)blockIdx.x * C;
     for (uint32_t i = threadIdx.x; i < C; i += blockDim.x) sh[i] = 0u;
+    const uint32_t *stab = stage_key_table(g, tab, sh + C);
     __syncthreads();
     const int64_t lo = tb[blockIdx.x], hi = tb[blockIdx.x + 1];
     for (int64_t base = lo; base < hi; base += U * (int64_t)blockDim.x) {
@@ -394,7 +445,10 @@ __global__ void __launch_bounds__(256, 4) k_scatter_tile(Geom g, const uint32_t 
             if (act[u]) rec_load<F32>(s64, s32, sid, i, r[u]);
         }
 #pragma unroll
-        for (int u = 0; u < U; ++u) key[u] = act[u] ? rec_key<F32>(g, tab, r[u], d) : 0u;
+        for (int u = 0; u < U; ++u) {
+            if constexpr (F32) key[u] = act[u] ? shared_key(g, stab, r[u].cell, d) : 0u;
+            else key[u] = act[u] ? shared_key_xyz<F32>(g, stab, r[u].a[0], r[u].a[1], r[u].a[2], d) : 0u;
+        }
         RunBump b[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) b[u] = tile_run_bump(sh, imm, key[u], k0, C, act[u]);
@@ -656,8 +710,9 @@ void materialize_records(ohpic_ctx *c)
     c->rec_pending = false;
 }
 
-// Largest tile (cells) whose counters the tile-local re-sort keeps in shared memory.
-constexpr int kTileSortMaxCells = 8192;
+// Shared memory of the tile-local re-sort (the tile's counters and the key table)
+// stays within the default 48 KB per CTA.
+constexpr size_t kTileSortMaxShared = 48 * 1024;
 
 // Re-sort of particles already sorted on the current tiling (tile_begin valid):
 // per species, tile-local counts, the scan of stayers + immigrants, tile starts,
@@ -668,7 +723,7 @@ static void sort_tiles(ohpic_ctx *c)
     const Geom &g = c->g;
     const bool f32 = c->cfg.precision == OHPIC_FP32;
     const int src = c->cur, dst = 1 - c->cur;
-    const size_t smem = sizeof(uint32_t) * (size_t)g.tile_cells;
+    const size_t smem = sizeof(uint32_t) * ((size_t)g.tile_cells + g.nx + g.ny + g.nz);
     for (int s = 0; s < c->cfg.nspecies; ++s) {
         const int64_t n = c->count[s];
         int64_t *tb = c->tile_begin + (int64_t)s * (g.ntile + 1);
@@ -712,7 +767,7 @@ int sort_particles(ohpic_ctx *c)
     const int axes = g.nx + g.ny + g.nz;
     k_key_table<<<(unsigned)((axes + 255) / 256), 256, 0, c->stream>>>(g, c->key_table);
     ++c->launches;
-    if (c->sorted && g.tile_cells <= kTileSortMaxCells) {
+    if (c->sorted && sizeof(uint32_t) * ((size_t)g.tile_cells + axes) <= kTileSortMaxShared) {
         sort_tiles(c);
         c->steps_since_sort = 0;
         return OHPIC_OK;
