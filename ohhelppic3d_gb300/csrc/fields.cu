@@ -223,6 +223,30 @@ __device__ __forceinline__ float node_rho(const unsigned long long *w, int64_t s
     return (float)(acc * kWeightUnit);
 }
 
+// node_rho of one or two species whose weight sums are already in registers.
+__device__ __forceinline__ float node_rho2(const unsigned long long W[2], int nsp, const double *q, const RhoScale &r)
+{
+    if (r.ok) {
+        __int128 acc = 0;
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            const long long m = s < nsp ? r.m[s] : 0;
+            if (m == 0) continue;
+            const unsigned long long am = (unsigned long long)(m < 0 ? -m : m);
+            unsigned __int128 p = ((unsigned __int128)__umul64hi(am, W[s]) << 64) | (unsigned __int128)(am * W[s]);
+            p <<= r.shift[s];
+            acc = m < 0 ? acc - (__int128)p : acc + (__int128)p;
+        }
+        float v;
+        if (i128_to_float_rne(acc, r.K, v)) return v;
+    }
+    double acc = 0.0;
+#pragma unroll
+    for (int s = 0; s < 2; ++s)
+        if (s < nsp) acc += q[s] * (double)W[s];
+    return (float)(acc * kWeightUnit);
+}
+
 // ---- pooled fields: many runs of one grid size, slot = blockIdx.y; on[slot] == 0 skips ----
 
 // rho of every active slot from its fixed-point weight sums (nsp species per slot,
@@ -344,13 +368,33 @@ struct SpeciesCharges {
     int nspecies;
 };
 
+// Four nodes per thread per iteration, every weight-sum load of the four issued
+// before the first node is formed: one node at a time, the kernel waited on two
+// dependent-free loads per node and ran at a third of its bytes' bandwidth.
 __global__ void k_wsum_to_rho(const unsigned long long *w, int64_t ncell, SpeciesCharges sc, float *rho)
 {
+    constexpr int U = 4;
     __shared__ RhoScale r;
     if (threadIdx.x == 0) r = rho_scale(sc.q, sc.nspecies);
     __syncthreads();
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ncell; t += (int64_t)gridDim.x * blockDim.x)
-        rho[t] = node_rho(w + t, ncell, sc.nspecies, sc.q, r);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ncell; t += U * stride) {
+        unsigned long long W[U][2];
+        bool in[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t i = t + u * stride;
+            in[u] = i < ncell;
+            W[u][0] = in[u] ? w[i] : 0ull;
+            W[u][1] = in[u] && sc.nspecies > 1 ? w[ncell + i] : 0ull;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (!in[u]) continue;
+            const int64_t i = t + u * stride;
+            rho[i] = sc.nspecies <= 2 ? node_rho2(W[u], sc.nspecies, sc.q, r) : node_rho(w + i, ncell, sc.nspecies, sc.q, r);
+        }
+    }
 }
 
 // FP64 form: rho = (sum_s q_s W_s) 2^-48 from the species' 2^-48 fixed-point
