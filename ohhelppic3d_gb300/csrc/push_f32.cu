@@ -195,22 +195,23 @@ __device__ __forceinline__ void fixed_weights2(float2 ox, float2 oy, float2 oz, 
     split_weights(fx1.y, f11.y, f01.y, z00.y, z10.y, z01.y, z11.y, u1);
 }
 
+// Node indices in 32 bits: the packed cell limits the FP32 form's grid to 2^32
+// nodes, so every index and partial sum fits an unsigned word.
 __device__ __forceinline__ void deposit_global_fixed(const Geom &g, unsigned long long *w, int ix, int iy, int iz,
                                                      const unsigned u[8])
 {
-    const int ix1 = ix + 1 == g.nx ? 0 : ix + 1;
-    const int iy1 = iy + 1 == g.ny ? 0 : iy + 1;
-    const int iz1 = iz + 1 == g.nz ? 0 : iz + 1;
-    const int64_t y0 = (int64_t)iy * g.nx, y1 = (int64_t)iy1 * g.nx;
-    const int64_t z0 = (int64_t)iz * g.nx * g.ny, z1 = (int64_t)iz1 * g.nx * g.ny;
-    atomicAdd(w + ix + y0 + z0, (unsigned long long)u[0]);
-    atomicAdd(w + ix1 + y0 + z0, (unsigned long long)u[1]);
-    atomicAdd(w + ix + y1 + z0, (unsigned long long)u[2]);
-    atomicAdd(w + ix1 + y1 + z0, (unsigned long long)u[3]);
-    atomicAdd(w + ix + y0 + z1, (unsigned long long)u[4]);
-    atomicAdd(w + ix1 + y0 + z1, (unsigned long long)u[5]);
-    atomicAdd(w + ix + y1 + z1, (unsigned long long)u[6]);
-    atomicAdd(w + ix1 + y1 + z1, (unsigned long long)u[7]);
+    const unsigned nx = (unsigned)g.nx, nxy = (unsigned)g.nx * (unsigned)g.ny;
+    const unsigned x0 = (unsigned)ix, x1 = ix + 1 == g.nx ? 0u : (unsigned)ix + 1u;
+    const unsigned y0 = (unsigned)iy * nx, y1 = (iy + 1 == g.ny ? 0u : (unsigned)iy + 1u) * nx;
+    const unsigned z0 = (unsigned)iz * nxy, z1 = (iz + 1 == g.nz ? 0u : (unsigned)iz + 1u) * nxy;
+    atomicAdd(w + (x0 + y0 + z0), (unsigned long long)u[0]);
+    atomicAdd(w + (x1 + y0 + z0), (unsigned long long)u[1]);
+    atomicAdd(w + (x0 + y1 + z0), (unsigned long long)u[2]);
+    atomicAdd(w + (x1 + y1 + z0), (unsigned long long)u[3]);
+    atomicAdd(w + (x0 + y0 + z1), (unsigned long long)u[4]);
+    atomicAdd(w + (x1 + y0 + z1), (unsigned long long)u[5]);
+    atomicAdd(w + (x0 + y1 + z1), (unsigned long long)u[6]);
+    atomicAdd(w + (x1 + y1 + z1), (unsigned long long)u[7]);
 }
 
 // Shared box: E nodes (float4) then the low and high words of the weight sums.
@@ -490,14 +491,13 @@ __device__ __forceinline__ float3 gather_box(const float4 *sE, const Box &b, int
 }
 
 // Offset o in cell units after the move: the integer part goes to the cell
-// index, o keeps the fraction in [0, 1).  o - floor(o) rounds to 1 for a tiny
-// negative o, which is the next cell's 0.
+// index, o keeps the fraction in [0, 1).  o - floor(o) rounds to 1 for a
+// negative o closer to 0 than half an ulp of 1; that particle keeps the lower
+// cell at the largest offset below 1, a position within FP32 rounding of its
+// true one like every other (one min instead of a test, a select and an add).
 __device__ __forceinline__ void carry(float &o, float f, int &i)
 {
-    if (o >= 1.f) {
-        o = 0.f;
-        f += 1.f;
-    }
+    o = fminf(o, 0x1.fffffep-1f);
     i += (int)f;
 }
 
