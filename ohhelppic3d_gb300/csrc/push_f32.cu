@@ -453,32 +453,44 @@ struct Tally {
     float ke = 0.f, px = 0.f, py = 0.f, pz = 0.f;
 };
 
-// One particle's E at its 8 nodes (staged box when key >= 0, else global
-// memory), interpolated with component C of the pair weights ww.
+// One particle's E at its 8 nodes, interpolated with component C of the pair
+// weights ww: from the staged box when key >= 0, else from the padded global E
+// (the particle left its box; nout counts it when `outside`).  The global node
+// index is 32-bit whenever the padded grid has at most 2^32 nodes.
 template <int C>
-__device__ __forceinline__ float3 gather1(const TileArgs &a, const Box &box, int key, int ix, int iy, int iz,
-                                          const float4 *sE, const float2 ww[8])
+__device__ __forceinline__ float3 gather1(const TileArgs &a, const Box &box, int key, bool outside, int ix, int iy,
+                                          int iz, const float4 *sE, const float2 ww[8], unsigned &nout)
 {
     float4 nd[8];
-    load_nodes<float4>(a, box, key, ix, iy, iz, sE, nd);
-    float ex = 0.f, ey = 0.f, ez = 0.f;
-#pragma unroll
-    for (int n = 0; n < 8; ++n) {
-        const float w = C == 0 ? ww[n].x : ww[n].y;
-        ex = fmaf(nd[n].x, w, ex);
-        ey = fmaf(nd[n].y, w, ey);
-        ez = fmaf(nd[n].z, w, ez);
+    if (key >= 0) {
+        const float4 *q = sE + key;
+        nd[0] = q[0];
+        nd[1] = q[1];
+        nd[2] = q[box.sx];
+        nd[3] = q[box.sx + 1];
+        nd[4] = q[box.sxy];
+        nd[5] = q[box.sxy + 1];
+        nd[6] = q[box.sxy + box.sx];
+        nd[7] = q[box.sxy + box.sx + 1];
+    } else {
+        nout += outside;
+        const Geom &g = a.g;
+        const float4 *E = (const float4 *)a.epad;
+        const unsigned gx = (unsigned)g.gx, gxy = (unsigned)g.gx * (unsigned)g.gy;
+        const float4 *q;
+        if ((unsigned long long)gxy * (unsigned)g.gz <= 0xffffffffull)
+            q = E + ((unsigned)(ix + g.halo) + gx * (unsigned)(iy + g.halo) + gxy * (unsigned)(iz + g.halo));
+        else
+            q = E + (ix + g.halo) + (int64_t)gx * (iy + g.halo) + (int64_t)gxy * (iz + g.halo);
+        nd[0] = __ldg(q);
+        nd[1] = __ldg(q + 1);
+        nd[2] = __ldg(q + gx);
+        nd[3] = __ldg(q + gx + 1);
+        nd[4] = __ldg(q + gxy);
+        nd[5] = __ldg(q + gxy + 1);
+        nd[6] = __ldg(q + gxy + gx);
+        nd[7] = __ldg(q + gxy + gx + 1);
     }
-    return make_float3(ex, ey, ez);
-}
-
-// The same from the staged box alone (key >= 0).
-template <int C>
-__device__ __forceinline__ float3 gather_box(const float4 *sE, const Box &b, int key, const float2 ww[8])
-{
-    const float4 *q = sE + key;
-    const float4 nd[8] = {q[0], q[1], q[b.sx], q[b.sx + 1], q[b.sxy], q[b.sxy + 1], q[b.sxy + b.sx],
-                          q[b.sxy + b.sx + 1]};
     float ex = 0.f, ey = 0.f, ez = 0.f;
 #pragma unroll
     for (int n = 0; n < 8; ++n) {
@@ -532,7 +544,6 @@ __device__ __forceinline__ void advance_pair(const TileArgs &a, const Box &box, 
     float2 ox = make_float2(s0.ox, s1.ox), oy = make_float2(s0.oy, s1.oy), oz = make_float2(s0.oz, s1.oz);
     if (kGather) {
         const int key0 = box.key(ix0, iy0, iz0), key1 = box.key(ix1, iy1, iz1);
-        t.out += (unsigned)(v0 && key0 < 0) + (unsigned)(v1 && key1 < 0);
         float2 wx0, wx1, wy0, wy1, wz0, wz1;
         cic2<W>(ox, wx0, wx1);
         cic2<W>(oy, wy0, wy1);
@@ -540,8 +551,9 @@ __device__ __forceinline__ void advance_pair(const TileArgs &a, const Box &box, 
         const float2 a00 = mul2(wx0, wy0), a10 = mul2(wx1, wy0), a01 = mul2(wx0, wy1), a11 = mul2(wx1, wy1);
         const float2 ww[8] = {mul2(a00, wz0), mul2(a10, wz0), mul2(a01, wz0), mul2(a11, wz0),
                               mul2(a00, wz1), mul2(a10, wz1), mul2(a01, wz1), mul2(a11, wz1)};
-        const float3 e0 = gather1<0>(a, box, e_ok ? key0 : -1, ix0, iy0, iz0, sE, ww);
-        const float3 e1 = gather1<1>(a, box, e_ok ? key1 : -1, ix1, iy1, iz1, sE, ww);
+        // (a slot past the count has the stand-in cell, inside the box)
+        const float3 e0 = gather1<0>(a, box, e_ok ? key0 : -1, key0 < 0, ix0, iy0, iz0, sE, ww, t.out);
+        const float3 e1 = gather1<1>(a, box, e_ok ? key1 : -1, key1 < 0, ix1, iy1, iz1, sE, ww, t.out);
         if (MODE == MODE_INTERP) {
             double *o = a.interp_out + 3 * idx;
             if (v0) { o[0] = e0.x; o[1] = e0.y; o[2] = e0.z; }
