@@ -55,10 +55,10 @@ PUSH_BYTES_PER_NODE = {"fp32": 12 + 4, "fp64": 24 + 8}
 STEP_BYTES_PER_NODE = {"fp32": 72, "fp64": 144}
 # DRAM traffic of one push launch over its algorithmic bytes, from one ncu capture of
 # the push one step after a sort (dram__bytes_read.sum + dram__bytes_write.sum) at
-# 128x128x64 with the same tuned tile, halo and particle density: 3.799 / 3.775 GB
+# 128x128x64 with the same tuned tile, halo and particle density: 3.800 / 3.775 GB
 # (FP32) and 6.812 / 6.476 GB (FP64, two steps after a sort).  Both terms scale with
 # the grid at fixed density, so the ratio carries to 256^3.
-PUSH_TRAFFIC_RATIO = {"fp32": 3.798875 / 3.774873600, "fp64": 6.811622 / 6.476005376}
+PUSH_TRAFFIC_RATIO = {"fp32": 3.799695 / 3.774873600, "fp64": 6.812251 / 6.476005376}
 PUSH_TRAFFIC_SOURCE = {
     "fp32": "ncu DRAM bytes of one push launch at 128x128x64 (same tile, halo and density), scaled by particles",
     "fp64": "ncu DRAM bytes of one push launch at 128x128x64 (same tile, halo and density), scaled by particles",
