@@ -74,9 +74,15 @@ __device__ __forceinline__ void box_add8(unsigned *hi, unsigned *lo, int key, in
     unsigned old[8];
 #pragma unroll
     for (int v = 0; v < 8; ++v) old[v] = atomicAdd(lo + key + off[v], u[v]);
+    // Carries are rare: one test for all eight, then the eight high-word adds
+    // (of 0 or 1) without a branch each.
+    unsigned cm = 0u;
 #pragma unroll
-    for (int v = 0; v < 8; ++v)
-        if (old[v] + u[v] < old[v]) atomicAdd(hi + key + off[v], 1u);
+    for (int v = 0; v < 8; ++v) cm |= (unsigned)(old[v] + u[v] < old[v]) << v;
+    if (cm) {
+#pragma unroll
+        for (int v = 0; v < 8; ++v) atomicAdd(hi + key + off[v], (cm >> v) & 1u);
+    }
 }
 
 // Adds u (weights, key = box index of the cell or < 0) to the shared box.  DEP
