@@ -10,11 +10,13 @@ most 128 x 128 x 64 cells) holding the same particles per cell; CTAs per tile
 only matter when the grid has few tiles, where the proxy is the grid itself.
 
 Search: from the library defaults, particles per lane, deposit reduction,
-every (tile shape, halo) pair, particles per lane again, split -- each candidate timed
-as the mean fused-push time over `steps` steps after a sort (a whole sort cycle
-ranks the shapes as a long run sees them: particles drift out of their tiles
-between sorts, which favours larger halos late in the cycle); then the sort
-cadence K minimising (sort time + sum of push times over K steps) / K.
+every (tile shape, halo) pair, deposit reduction and particles per lane again,
+split -- each candidate timed as the mean fused-push time over `steps` steps
+after a sort (a whole sort cycle ranks the shapes as a long run sees them:
+particles drift out of their tiles between sorts, which favours larger halos
+late in the cycle), and kept only when it beats the current choice by more
+than the noise; then the sort cadence K minimising (sort time + sum of push
+times over K steps) / K.
 """
 from __future__ import annotations
 
@@ -77,13 +79,14 @@ def _sort_ms(ctx: PicContext) -> float:
 
 
 def tune(n, dt, b0, qm, q, capacity_per_cell, species, precision=FP32, weights=0, proxy=True,
-         steps=3, max_cadence=40, log=None, proxy_limit=(128, 128, 64)) -> dict:
+         steps=3, max_cadence=40, log=None, proxy_limit=(128, 128, 64), keep=0.01) -> dict:
     """Returns the best tuning dict for a run on grid n.
 
     species: list of SpeciesInit (device injector parameters) of the run;
     capacity_per_cell: particles per cell to reserve per species (>= ppc);
     proxy_limit: the largest proxy grid.  A proxy with many tiles per SM ranks
-    tile shapes as the full grid does; a small one favours small tiles."""
+    tile shapes as the full grid does; a small one favours small tiles.
+    keep: the margin by which a candidate must beat the current choice."""
     grid = proxy_grid(n, proxy_limit) if proxy else tuple(n)
     ncell = grid[0] * grid[1] * grid[2]
     caps = [int(c * ncell) + 1024 for c in capacity_per_cell]
@@ -105,16 +108,26 @@ def tune(n, dt, b0, qm, q, capacity_per_cell, species, precision=FP32, weights=0
         return ms
 
     def joint(candidates):
-        """Measures every candidate (a dict of tuning keys) on top of the current best."""
+        """Measures every candidate (a dict of tuning keys) on top of the current
+        best.  A candidate replaces the current best only when it beats the current
+        best's own time in this pass by more than `keep` (run-to-run noise of a few
+        steps on the proxy is about 1%), so near-ties do not flip the choice."""
         nonlocal best
         base = dict(best)
         scores = []
+        incumbent = None
         for cand in candidates:
             s = measure(**{**base, **cand})
-            if s is not None:
-                scores.append((s, cand))
+            if s is None:
+                continue
+            scores.append((s, cand))
+            if all(base.get(k) == v or (isinstance(v, (tuple, list)) and tuple(base.get(k, ())) == tuple(v))
+                   for k, v in cand.items()):
+                incumbent = s
         if scores:
-            best = {**base, **min(scores, key=lambda x: x[0])[1]}
+            s, cand = min(scores, key=lambda x: x[0])
+            if incumbent is None or s < incumbent * (1.0 - keep):
+                best = {**base, **cand}
             ctx.set_tuning(**best)
 
     def descend(key, values):
@@ -128,8 +141,16 @@ def tune(n, dt, b0, qm, q, capacity_per_cell, species, precision=FP32, weights=0
         # drift before they leave the staged box, and with the tile it sets the
         # shared memory per CTA, so a small tile with a wide halo can beat both a
         # wide halo alone and a large tile alone
-        joint([{"tile": t, "halo": h} for t in _tiles(grid) for h in (1, 2, 3)])
+        # (with the LANES deposit too when the first pass chose another: the
+        # LANES push of the common box shapes has kernels compiled for them)
+        deps = [best["deposit"]]
+        if precision == FP32 and best["deposit"] != DEPOSIT_LANES:
+            deps.append(DEPOSIT_LANES)
+        joint([{"tile": t, "halo": h, "deposit": d} for t in _tiles(grid) for h in (1, 2, 3) for d in deps])
         if precision == FP32:
+            # again on the chosen box: the deposit reduction's cost depends on the
+            # tile (particles per cell run, the shape's compiled kernels)
+            descend("deposit", [DEPOSIT_LANES, DEPOSIT_RUNS, DEPOSIT_GROUPS, DEPOSIT_UNIFORM, DEPOSIT_MATCH])
             descend("lane_particles", [2, 4])
         if not proxy or grid == tuple(n):
             descend("split", [1, 2, 4, 8])

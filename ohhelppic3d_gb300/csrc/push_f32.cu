@@ -41,6 +41,12 @@
 namespace ohpic {
 namespace {
 
+// The launch shape the autotuner picks for the dense plasmas (tile 16 x 8 x 8
+// cells, halo 2) has its own push kernels with the box geometry fixed at
+// compile time: node offsets become immediates of the shared-memory loads and
+// atomics instead of registers and adds.
+constexpr int kFixTx = 16, kFixTy = 8, kFixTz = 8, kFixHalo = 2;
+
 // Segmented sum of u over runs of equal keys held by adjacent lanes (at most 5
 // shuffle steps, stopping early when the runs are short); returns true in the
 // run's first lane, which then holds the run total.
@@ -74,14 +80,16 @@ __device__ __forceinline__ void box_add8(unsigned *hi, unsigned *lo, int key, in
     unsigned old[8];
 #pragma unroll
     for (int v = 0; v < 8; ++v) old[v] = atomicAdd(lo + key + off[v], u[v]);
-    // Carries are rare: one test for all eight, then the eight high-word adds
-    // (of 0 or 1) without a branch each.
-    unsigned cm = 0u;
+    // A carry needs old + u >= 2^32, so old or u at least 2^31: one test of the
+    // words' OR rules carries out for all eight (node sums stay far below 2^31
+    // units, 128 particle weights, in any plasma of sane density); past it the
+    // eight high-word adds (of 0 or 1) go without a branch each.
+    unsigned m = 0u;
 #pragma unroll
-    for (int v = 0; v < 8; ++v) cm |= (unsigned)(old[v] + u[v] < old[v]) << v;
-    if (cm) {
+    for (int v = 0; v < 8; ++v) m |= old[v] | u[v];
+    if (m >> 31) {
 #pragma unroll
-        for (int v = 0; v < 8; ++v) atomicAdd(hi + key + off[v], (cm >> v) & 1u);
+        for (int v = 0; v < 8; ++v) atomicAdd(hi + key + off[v], (unsigned)(old[v] + u[v] < old[v]));
     }
 }
 
@@ -174,14 +182,16 @@ __device__ __forceinline__ void cic2(float2 r, float2 &w0, float2 &w1)
 // sibling is the difference, so every weight is non-negative and the eight add
 // up to 2^24 with no fix-up pass (7 float-to-integer conversions instead of 8).
 // The products come in for a pair of particles (component c of each argument).
+// Y11 and Z11 need no clamp: f11 = fx1 * wy1 and z11 = f11 * wz1 with weights in
+// [0, 1], and rounding is monotonic, so round(z11) <= round(f11) <= round(fx1).
 __device__ __forceinline__ void split_weights(float fx1, float f11, float f01, float z00, float z10, float z01,
                                               float z11, unsigned u[8])
 {
     const unsigned X1 = __float2uint_rn(fx1), X0 = (1u << 24) - X1;
-    const unsigned Y11 = min(__float2uint_rn(f11), X1), Y01 = min(__float2uint_rn(f01), X0);
+    const unsigned Y11 = __float2uint_rn(f11), Y01 = min(__float2uint_rn(f01), X0);
     const unsigned Y10 = X1 - Y11, Y00 = X0 - Y01;
     const unsigned Z00 = min(__float2uint_rn(z00), Y00), Z10 = min(__float2uint_rn(z10), Y10);
-    const unsigned Z01 = min(__float2uint_rn(z01), Y01), Z11 = min(__float2uint_rn(z11), Y11);
+    const unsigned Z01 = min(__float2uint_rn(z01), Y01), Z11 = __float2uint_rn(z11);
     u[0] = Y00 - Z00; u[1] = Y10 - Z10; u[2] = Y01 - Z01; u[3] = Y11 - Z11;
     u[4] = Z00; u[5] = Z10; u[6] = Z01; u[7] = Z11;
 }
@@ -761,7 +771,7 @@ __device__ __forceinline__ void tile_pass(const TileArgs &a, const PartF32 &p, c
 // the lanes' last sums once per 128 particles.  The per-particle arithmetic is
 // advance_pair(), as in the two-per-lane pass, and every sum is integer, so both
 // passes give the same bits.
-template <int MODE, int DEP, int W, bool REC = false>
+template <int MODE, int DEP, int W, bool REC = false, bool FIX = false>
 __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap,
                                            const Item &it, unsigned char *smem, uint64_t *ebar,
                                            const RecIn &rin = RecIn{})
@@ -772,8 +782,16 @@ __device__ __forceinline__ void tile_pass4(const TileArgs &a, const PartF32 &p, 
     constexpr bool kMove = MODE == MODE_PUSH;
 
     const Geom &g = a.g;
-    const Box box = make_box(g, it);
-    const int s3 = g.sx * g.sy * g.sz;
+    Box box = make_box(g, it);
+    if constexpr (FIX) {
+        // the box of tile (16,8,8) with halo 2, its spans and pitches immediates
+        box.spx = kFixTx + 2 * kFixHalo;
+        box.spy = kFixTy + 2 * kFixHalo;
+        box.spz = kFixTz + 2 * kFixHalo;
+        box.sx = kFixTx + 2 * kFixHalo + 1;
+        box.sxy = box.sx * (kFixTy + 2 * kFixHalo + 1);
+    }
+    const int s3 = FIX ? box.sxy * (kFixTz + 2 * kFixHalo + 1) : g.sx * g.sy * g.sz;
     float4 *sE = (float4 *)smem;
     unsigned *slo = (unsigned *)(smem + (kGather ? (size_t)s3 * sizeof(float4) : 0));
     unsigned *shi = slo + s3;
@@ -886,31 +904,32 @@ __device__ __forceinline__ unsigned char *align128(unsigned char *p)
 }
 
 // Work item b with PPL particles per lane: 2 (every mode) or 4 (push and deposit).
-template <int MODE, int DEP, int PPL, int W>
+template <int MODE, int DEP, int PPL, int W, bool FIX = false>
 __device__ __forceinline__ void run_item(const TileArgs &a, const PartF32 &p, const CUtensorMap *emap, int64_t b,
                                          unsigned char *smem, uint64_t *ebar)
 {
     Item it;
     if constexpr (PPL == 4) {
-        if (get_item<4>(a, b, it)) tile_pass4<MODE, DEP, W>(a, p, emap, it, smem, ebar);
+        if (get_item<4>(a, b, it)) tile_pass4<MODE, DEP, W, false, FIX>(a, p, emap, it, smem, ebar);
     } else {
         if (get_item<2>(a, b, it)) tile_pass<MODE, DEP, W>(a, p, emap, it, smem, ebar);
     }
 }
 
-// One context: one CTA per work item.
-template <int MODE, int DEP, int PPL, int W>
+// One context: one CTA per work item.  FIX: the launch's tile is (16,8,8) with
+// halo 2, so the box spans and pitches are compile-time constants.
+template <int MODE, int DEP, int PPL, int W, bool FIX = false>
 __global__ void __launch_bounds__(256, 2) tiled_f32(TileArgs a, PartF32 p, const __grid_constant__ CUtensorMap emap)
 {
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t ebar;
     // box start aligned to 128 bytes (the launch reserves the slack)
-    run_item<MODE, DEP, PPL, W>(a, p, &emap, (int64_t)blockIdx.x, align128(smem_raw), &ebar);
+    run_item<MODE, DEP, PPL, W, FIX>(a, p, &emap, (int64_t)blockIdx.x, align128(smem_raw), &ebar);
 }
 
 // The push right after a sort, reading the sort's records (four per lane, LANES
 // deposit: the default launch shape); writes the word arrays p and the ids.
-template <int W>
+template <int W, bool FIX>
 __global__ void __launch_bounds__(256, 2) tiled_f32_rec(TileArgs a, PartF32 p, RecIn rin,
                                                         const __grid_constant__ CUtensorMap emap)
 {
@@ -918,7 +937,7 @@ __global__ void __launch_bounds__(256, 2) tiled_f32_rec(TileArgs a, PartF32 p, R
     __shared__ __align__(8) uint64_t ebar;
     Item it;
     if (get_item<4>(a, (int64_t)blockIdx.x, it))
-        tile_pass4<MODE_PUSH, OHPIC_DEPOSIT_LANES, W, true>(a, p, &emap, it, align128(smem_raw), &ebar, rin);
+        tile_pass4<MODE_PUSH, OHPIC_DEPOSIT_LANES, W, true, FIX>(a, p, &emap, it, align128(smem_raw), &ebar, rin);
 }
 
 // Many contexts in one persistent launch.  Every CTA takes the next item from
@@ -1021,11 +1040,13 @@ static auto by_weights(int w, F f)
 void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks, size_t smem, const RecIn *rin)
 {
     const PartF32 &pp = c->p32[c->cur];
+    const Geom &g = a.g;
+    const bool fix = g.tx == kFixTx && g.ty == kFixTy && g.tz == kFixTz && g.halo == kFixHalo;
     by_weights(a.weights, [&](auto w) {
         constexpr int W = decltype(w)::value;
         if (rin) {
             if (blocks <= 0) return 0;
-            auto kernel = tiled_f32_rec<W>;
+            auto kernel = fix ? tiled_f32_rec<W, true> : tiled_f32_rec<W, false>;
             cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (smem > 96 * 1024)
                 cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -1038,7 +1059,9 @@ void launch_tiled_f32(ohpic_ctx *c, const TileArgs &a, int mode, int64_t blocks,
             by_lanes(a.ppl, [&](auto l) {
                 return by_deposit(a.deposit, [&](auto d) {
                     constexpr int D = decltype(d)::value, L = decltype(l)::value;
-                    if (mode == MODE_PUSH) launch_k(c, tiled_f32<MODE_PUSH, D, L, W>, a, blocks, smem, pp);
+                    if (mode == MODE_PUSH && L == 4 && D == OHPIC_DEPOSIT_LANES && fix)
+                        launch_k(c, tiled_f32<MODE_PUSH, D, L, W, true>, a, blocks, smem, pp);
+                    else if (mode == MODE_PUSH) launch_k(c, tiled_f32<MODE_PUSH, D, L, W>, a, blocks, smem, pp);
                     else launch_k(c, tiled_f32<MODE_DEPOSIT, D, L, W>, a, blocks, smem, pp);
                     return 0;
                 });

@@ -107,3 +107,52 @@ def test_search_keeps_the_defaults_when_every_candidate_is_refused(monkeypatch):
                   species=[None], steps=2, max_cadence=5)
     assert best["trials"] == []
     assert tuple(best["tile"]) == (8, 8, 8) and best["halo"] == 1
+
+
+def test_near_ties_keep_the_current_choice_and_deposit_is_retuned_on_the_box(monkeypatch):
+    """RUNS is 0.5% faster than LANES on the default box (a near-tie: kept at
+    LANES), and on the (16,8,8) box LANES is much faster than RUNS: whatever the
+    first deposit pass picks, the tile pass (run with LANES as well) and the
+    second deposit pass must end at (16,8,8) with LANES."""
+    def cost2(t, since_sort):
+        c = cost(t, since_sort)
+        lanes = t["deposit"] == P.DEPOSIT_LANES
+        if tuple(t["tile"]) == (16, 8, 8):
+            c += 0.0 if lanes else 1.5
+        else:
+            c -= 0.7 if not lanes else 0.0       # undo the model's LANES advantage
+            c += -0.05 if t["deposit"] == P.DEPOSIT_RUNS else 0.0
+        return c
+
+    class Ctx2(FakeCtx):
+        def step(self, dt, n=1):
+            for _ in range(n):
+                if self.timing:
+                    self.push_ms += cost2(self.t, self.since)
+                    self.push_launches += 1
+                self.since += 1
+
+    def start():
+        c = Ctx2()
+        c.t["deposit"] = P.DEPOSIT_LANES
+        return c
+
+    monkeypatch.setattr(A, "_ctx", lambda cfg_kw, species, seed=(42, 4242): start())
+    monkeypatch.setattr(A, "_sort_ms", lambda ctx: 1.0)
+    best = A.tune(n=(64, 32, 32), dt=0.1, b0=(0, 0, 0.5), qm=[-1.0], q=[1.0], capacity_per_cell=[9.0],
+                  species=[None], steps=4, max_cadence=5)
+    assert tuple(best["tile"]) == (16, 8, 8)
+    assert best["deposit"] == P.DEPOSIT_LANES
+    # the first deposit pass (on the default (8,8,8) box) measured RUNS 0.5% faster
+    # than LANES and kept LANES
+    first = [tr for tr in best["trials"] if tuple(tr["tile"]) == (8, 8, 8)]
+    assert any(tr["deposit"] == P.DEPOSIT_RUNS for tr in first)
+
+    # with no margin, the near-tie flips the first pass to RUNS; the tile pass
+    # still finds (16,8,8) with LANES
+    monkeypatch.setattr(A, "_ctx", lambda cfg_kw, species, seed=(42, 4242): start())
+    best0 = A.tune(n=(64, 32, 32), dt=0.1, b0=(0, 0, 0.5), qm=[-1.0], q=[1.0], capacity_per_cell=[9.0],
+                   species=[None], steps=4, max_cadence=5, keep=0.0)
+    assert tuple(best0["tile"]) == (16, 8, 8) and best0["deposit"] == P.DEPOSIT_LANES
+    first0 = [tr for tr in best0["trials"] if tuple(tr["tile"]) == (8, 8, 8) and tr["halo"] == 1]
+    assert min(first0, key=lambda tr: tr["push_ms"])["deposit"] == P.DEPOSIT_RUNS

@@ -47,7 +47,8 @@ def test_fp32_state_identical_across_launch_shapes(ohpic):
     ref_f, ref_p, ref_d = _run(P, {})
     variants = [{"deposit": P.DEPOSIT_UNIFORM}, {"deposit": P.DEPOSIT_MATCH}, {"deposit": P.DEPOSIT_GROUPS},
                 {"deposit": P.DEPOSIT_RUNS}, {"lane_particles": 2, "deposit": P.DEPOSIT_LANES},
-                {"tile": (4, 4, 4)}, {"tile": (16, 8, 8), "deposit": P.DEPOSIT_GROUPS}, {"halo": 1},
+                {"tile": (4, 4, 4)}, {"tile": (16, 8, 8)}, {"tile": (16, 8, 8), "deposit": P.DEPOSIT_GROUPS},
+                {"halo": 1},
                 {"halo": 3}, {"split": 3}, {"sort_every": 1}, {"sort_every": 100},
                 {"lane_particles": 2}, {"lane_particles": 2, "deposit": P.DEPOSIT_UNIFORM},
                 {"lane_particles": 2, "deposit": P.DEPOSIT_GROUPS, "tile": (4, 4, 4)},
@@ -72,9 +73,10 @@ def test_fp32_particles_outside_their_box_identical(ohpic):
     base = {"tile": (8, 8, 8), "halo": 1}
     ref_f, ref_p, ref_d = _run(P, dict(base, sort_every=1), steps=24, vth=4.0)
     for v in (dict(base, sort_every=1000, lane_particles=4), dict(base, sort_every=1000, lane_particles=2),
+              dict(sort_every=1000, lane_particles=4, tile=(16, 8, 8), halo=2),
               dict(base, sort_every=1000, lane_particles=4, deposit=P.DEPOSIT_MATCH)):
         f, p, d = _run(P, v, steps=24, vth=4.0)
-        # the queue was exercised (a sorted run has only the few particles of the
+        # the global path was exercised (a sorted run has only the few particles of the
         # four-particle groups that straddle a tile boundary outside)
         assert d["outside_tile"] > 1000 + 10 * ref_d["outside_tile"], (v, d["outside_tile"])
         for w in f:
@@ -99,7 +101,7 @@ def test_autotuner_returns_a_valid_shape(ohpic):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("tuning", [{}, {"halo": 1, "split": 2}, {"deposit": "RUNS"}])
+@pytest.mark.parametrize("tuning", [{}, {"halo": 1, "split": 2}, {"deposit": "RUNS"}, {"tile": (16, 8, 8)}])
 def test_push_from_sort_records_matches_arrays(ohpic, tuning):
     """The FP32 sort leaves its 32-byte records pending and the next push (four
     per lane, LANES deposit) reads them and writes the word arrays and ids
