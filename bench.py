@@ -55,10 +55,10 @@ PUSH_BYTES_PER_NODE = {"fp32": 12 + 4, "fp64": 24 + 8}
 STEP_BYTES_PER_NODE = {"fp32": 72, "fp64": 144}
 # DRAM traffic of one push launch over its algorithmic bytes, from one ncu capture of
 # the push one step after a sort (dram__bytes_read.sum + dram__bytes_write.sum) at
-# 128x128x64 with the same tuned tile, halo and particle density: 3.800 / 3.775 GB
+# 128x128x64 with the same tuned tile, halo and particle density: 3.801 / 3.775 GB
 # (FP32) and 6.812 / 6.476 GB (FP64, two steps after a sort).  Both terms scale with
 # the grid at fixed density, so the ratio carries to 256^3.
-PUSH_TRAFFIC_RATIO = {"fp32": 3.799695 / 3.774873600, "fp64": 6.812251 / 6.476005376}
+PUSH_TRAFFIC_RATIO = {"fp32": 3.801085 / 3.774873600, "fp64": 6.812251 / 6.476005376}
 PUSH_TRAFFIC_SOURCE = {
     "fp32": "ncu DRAM bytes of one push launch at 128x128x64 (same tile, halo and density), scaled by particles",
     "fp64": "ncu DRAM bytes of one push launch at 128x128x64 (same tile, halo and density), scaled by particles",
@@ -226,7 +226,7 @@ def tune_form(P, wl, form, args, weights) -> dict | None:
                       precision=P.FP32 if form == "fp32" else P.FP64, weights=weights,
                       steps=max(4, wl.sort_every - 1) if form == "fp32" else 4,
                       max_cadence=40, proxy_limit=(256, 128, 64))
-    keep = ("tile", "halo", "split", "deposit", "lane_particles")
+    keep = ("tile", "halo", "split", "deposit", "lane_particles", "sort_lead")
     return {**{k: t[k] for k in keep}, "sort_every_suggested": t["sort_every"],
             "tuned_on": list(t["grid_tuned_on"]), "trials": len(t["trials"]),
             "seconds": round(time.perf_counter() - t0, 2)}

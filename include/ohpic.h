@@ -266,6 +266,10 @@ typedef struct ohpic_tuning {
     int32_t deposit;            /* OHPIC_DEPOSIT_* (FP32 form) */
     int32_t sort_every;         /* cell sort cadence in steps; 0 = only explicit sorts */
     int32_t lane_particles;     /* FP32 push: consecutive particles per lane, 2 or 4 */
+    int32_t sort_lead;          /* FP32 form, 0..4096: the cell sort files each particle under
+                                   the cell it reaches after this many steps of straight-line
+                                   motion (0: its current cell), so that a sort cycle's
+                                   particles stay closer to their tile's staged box */
 } ohpic_tuning;
 int ohpic_get_tuning(ohpic_ctx *ctx, ohpic_tuning *out);
 /* Changing tile or halo re-lays out the staged E field: the next push solves

@@ -74,11 +74,13 @@ class Tuning(C.Structure):
     _fields_ = [
         ("tile", C.c_int32 * 3), ("halo", C.c_int32), ("split", C.c_int32),
         ("deposit", C.c_int32), ("sort_every", C.c_int32), ("lane_particles", C.c_int32),
+        ("sort_lead", C.c_int32),
     ]
 
     def as_dict(self) -> dict:
         return {"tile": tuple(self.tile), "halo": self.halo, "split": self.split,
-                "deposit": self.deposit, "sort_every": self.sort_every, "lane_particles": self.lane_particles}
+                "deposit": self.deposit, "sort_every": self.sort_every, "lane_particles": self.lane_particles,
+                "sort_lead": self.sort_lead}
 
 
 DEPOSIT_RUNS, DEPOSIT_UNIFORM, DEPOSIT_MATCH, DEPOSIT_GROUPS, DEPOSIT_LANES = 0, 1, 2, 3, 4
@@ -409,6 +411,7 @@ class PicContext:
         t.halo, t.split = int(cur["halo"]), int(cur["split"])
         t.deposit, t.sort_every = int(cur["deposit"]), int(cur["sort_every"])
         t.lane_particles = int(cur.get("lane_particles", 4))
+        t.sort_lead = int(cur.get("sort_lead", 0))
         self._check(lib().ohpic_set_tuning(self.ptr, C.byref(t)))
 
     def memory(self) -> int:

@@ -1,22 +1,22 @@
 """Autotuner for the launch shape of the particle kernels.
 
 Picks, per grid size and plasma, the tile shape, the halo staged around a tile,
-the CTAs per (species, tile), the FP32 particles per lane and warp-deposit
-reduction, and the cell-sort cadence.  It measures on a throwaway context filled by the device injector with
-the same particles per cell and physics as the run, so tuning never advances the
-caller's simulation.  The per-CTA work depends only on the tile and the plasma,
+the CTAs per (species, tile), the FP32 particles per lane, warp-deposit
+reduction and sort lead, and the cell-sort cadence.  It measures on a throwaway
+context filled by the device injector with the same particles per cell and
+physics as the run, so tuning never advances the caller's simulation.  The per-CTA work depends only on the tile and the plasma,
 not on the grid size, so large grids are tuned on a proxy grid (by default at
 most 128 x 128 x 64 cells) holding the same particles per cell; CTAs per tile
 only matter when the grid has few tiles, where the proxy is the grid itself.
 
-Search: from the library defaults, particles per lane, deposit reduction,
-every (tile shape, halo) pair, deposit reduction and particles per lane again,
-split -- each candidate timed as the mean fused-push time over `steps` steps
-after a sort (a whole sort cycle ranks the shapes as a long run sees them:
-particles drift out of their tiles between sorts, which favours larger halos
-late in the cycle), and kept only when it beats the current choice by more
-than the noise; then the sort cadence K minimising (sort time + sum of push
-times over K steps) / K.
+Search: from the library defaults, particles per lane, deposit reduction, sort
+lead (FP32), every (tile shape, halo) pair, deposit reduction, sort lead and
+particles per lane again, split -- each candidate timed as the mean fused-push
+time over `steps` steps after a sort (a whole sort cycle ranks the shapes as a
+long run sees them: particles drift out of their tiles between sorts, which
+favours larger halos late in the cycle), and kept only when it beats the
+current choice by more than the noise; then the sort cadence K minimising
+(sort time + sum of push times over K steps) / K.
 """
 from __future__ import annotations
 
@@ -133,10 +133,14 @@ def tune(n, dt, b0, qm, q, capacity_per_cell, species, precision=FP32, weights=0
     def descend(key, values):
         joint([{key: v} for v in values])
 
+    # sort leads (FP32 form): none, a quarter and half of the measured cycle, so
+    # that particles are filed where they are a quarter or half way through it
+    leads = sorted({0, (steps + 1) // 4, (steps + 1) // 2})
     try:
         if precision == FP32:
             descend("lane_particles", [2, 4])
             descend("deposit", [DEPOSIT_LANES, DEPOSIT_RUNS, DEPOSIT_GROUPS, DEPOSIT_UNIFORM, DEPOSIT_MATCH])
+            descend("sort_lead", leads)
         # tile and halo together: the halo's absolute width sets how far particles
         # drift before they leave the staged box, and with the tile it sets the
         # shared memory per CTA, so a small tile with a wide halo can beat both a
@@ -151,6 +155,7 @@ def tune(n, dt, b0, qm, q, capacity_per_cell, species, precision=FP32, weights=0
             # again on the chosen box: the deposit reduction's cost depends on the
             # tile (particles per cell run, the shape's compiled kernels)
             descend("deposit", [DEPOSIT_LANES, DEPOSIT_RUNS, DEPOSIT_GROUPS, DEPOSIT_UNIFORM, DEPOSIT_MATCH])
+            descend("sort_lead", leads)
             descend("lane_particles", [2, 4])
         if not proxy or grid == tuple(n):
             descend("split", [1, 2, 4, 8])
@@ -185,6 +190,7 @@ def apply(ctx: PicContext, tuning: dict, keep_sort_every: bool = False):
     ctx.set_tuning(tile=tuning.get("tile", cur["tile"]), halo=tuning.get("halo", cur["halo"]),
                    split=tuning.get("split", cur["split"]), deposit=tuning.get("deposit", cur["deposit"]),
                    lane_particles=tuning.get("lane_particles", cur["lane_particles"]),
+                   sort_lead=tuning.get("sort_lead", cur.get("sort_lead", 0)),
                    sort_every=cur["sort_every"] if keep_sort_every else tuning.get("sort_every", cur["sort_every"]))
 
 

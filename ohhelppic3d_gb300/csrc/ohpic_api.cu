@@ -384,6 +384,7 @@ int ohpic_create(const ohpic_config *cfg, ohpic_ctx **out)
     c->sc_dt = NAN;
     c->dep_strategy = OHPIC_DEPOSIT_LANES;
     c->lane_particles = 4;
+    c->sort_lead = 0;
     c->tma_polls = kTmaWaitPolls;
     Geom &g = c->g;
     if (!make_geom(k, tile, c->halo, g)) {
@@ -886,6 +887,7 @@ int ohpic_get_tuning(ohpic_ctx *c, ohpic_tuning *t)
     t->deposit = c->dep_strategy;
     t->lane_particles = c->lane_particles;
     t->sort_every = c->cfg.sort_every;
+    t->sort_lead = c->sort_lead;
     return OHPIC_OK;
 }
 
@@ -895,7 +897,9 @@ int ohpic_set_tuning(ohpic_ctx *c, const ohpic_tuning *t)
     if (t->split < 1 || t->split > 64 || t->deposit < OHPIC_DEPOSIT_RUNS || t->deposit > OHPIC_DEPOSIT_LANES ||
         t->sort_every < 0 || (t->lane_particles != 2 && t->lane_particles != 4))
         return fail(c, OHPIC_ERR_INVALID,
-                    "tuning: split 1..64, deposit 0..3, sort_every >= 0, lane_particles 2 or 4");
+                    "tuning: split 1..64, deposit 0..4, sort_every >= 0, lane_particles 2 or 4");
+    if (t->sort_lead < 0 || t->sort_lead > 4096 || (t->sort_lead != 0 && c->cfg.precision != OHPIC_FP32))
+        return fail(c, OHPIC_ERR_INVALID, "tuning: sort_lead 0..4096, nonzero only in the FP32 form");
     Geom g2;
     if (!make_geom(c->cfg, t->tile, t->halo, g2))
         return fail(c, OHPIC_ERR_INVALID, "tuning: tile edges must divide the grid (<= 64) and the staged box fit");
@@ -930,6 +934,7 @@ int ohpic_set_tuning(ohpic_ctx *c, const ohpic_tuning *t)
     c->dep_strategy = t->deposit;
     c->lane_particles = t->lane_particles;
     c->cfg.sort_every = t->sort_every;
+    c->sort_lead = t->sort_lead;
     return OHPIC_OK;
 }
 

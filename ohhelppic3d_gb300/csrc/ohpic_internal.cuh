@@ -268,6 +268,7 @@ struct ohpic_ctx {
     int halo;
     int dep_strategy;           // OHPIC_DEPOSIT_* for the FP32 warp deposit
     int lane_particles;         // FP32 push/deposit: particles per lane (2 or 4)
+    int sort_lead;              // FP32 sort: steps of straight-line motion the sort key anticipates
     uint32_t tma_polls;         // polls allowed for the staged E box (ohpic_set_tma_wait_limit)
     bool with_energy;
     bool kin_valid;             // diag->kin holds the sums of the current velocities

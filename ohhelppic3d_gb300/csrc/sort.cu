@@ -13,7 +13,10 @@
 // reads the records directly (push_f32.cu), or to materialize_records.  In the
 // scatter, lanes of a warp that share a key (grouped with __match_any_sync) take
 // consecutive slots in lane order, so a warp's relative order is kept; order
-// across warps follows the atomic order.
+// across warps follows the atomic order.  With a sort lead (FP32 form,
+// ohpic_tuning.sort_lead), the key is the cell each particle reaches after that
+// many steps of straight-line motion instead of its current cell.
+#include <cmath>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -68,13 +71,54 @@ __device__ __forceinline__ uint32_t cell_key(const Geom &g, const uint32_t *tab,
     return tile_key(g, ix, iy, iz);
 }
 
+// FP32 form, sort lead h > 0 (cells per unit velocity): a particle is filed
+// under the cell it reaches moving in a straight line for h, cell i + floor(o +
+// v h) per axis, wrapped into the grid.  Particles then sit, on average, in
+// their tile's box at the middle of a sort cycle instead of at its start, so
+// fewer of them leave the staged box by its end.  The histogram and the scatter
+// run this same sequence of explicitly rounded operations on the same words,
+// so they file every particle under the same key.
+__device__ __forceinline__ int lead_axis(int i, float o, float v, float h, int n)
+{
+    float f = floorf(__fmaf_rn(v, h, o));
+    f = fminf(fmaxf(f, -16777216.f), 16777216.f);   // |f| <= 2^24 (a NaN gives -2^24)
+    int k = i + (int)f;
+    if ((unsigned)k >= (unsigned)n) {
+        k %= n;
+        if (k < 0) k += n;
+    }
+    return k;
+}
+
+// Cell of a packed FP32 cell c with offsets f[0..2] and velocities f[3..5]
+// after the lead h (h == 0: the cell itself); a cell outside the grid flags
+// OHPIC_ERR_BOUNDS (site `site`) and sorts as cell 0.
+__device__ __forceinline__ void lead_cell(const Geom &g, int32_t c, const float f[6], float h, int site,
+                                          DevDiag *d, int &ix, int &iy, int &iz)
+{
+    ix = cell_x(c), iy = cell_y(c), iz = cell_z(c);
+    if ((unsigned)ix >= (unsigned)g.nx || (unsigned)iy >= (unsigned)g.ny || (unsigned)iz >= (unsigned)g.nz) {
+        if (atomicCAS(&d->err_code, 0, OHPIC_ERR_BOUNDS) == 0) d->err_info = site;
+        ix = iy = iz = 0;
+    }
+    if (h != 0.f) {
+        ix = lead_axis(ix, f[0], f[3], h, g.nx);
+        iy = lead_axis(iy, f[1], f[4], h, g.ny);
+        iz = lead_axis(iz, f[2], f[5], h, g.nz);
+    }
+}
+
 template <bool F32>
 __device__ __forceinline__ uint32_t particle_key(const Geom &g, const uint32_t *tab, const PartF64 &p64,
-                                                 const PartF32 &p32, int64_t i, DevDiag *d)
+                                                 const PartF32 &p32, int64_t i, float h, DevDiag *d)
 {
     if (F32) {
         const int32_t c = p32.cell[i];
-        return cell_key(g, tab, cell_x(c), cell_y(c), cell_z(c), d);
+        if (h == 0.f) return cell_key(g, tab, cell_x(c), cell_y(c), cell_z(c), d);
+        const float f[6] = {p32.ox[i], p32.oy[i], p32.oz[i], p32.vx[i], p32.vy[i], p32.vz[i]};
+        int ix, iy, iz;
+        lead_cell(g, c, f, h, 10, d, ix, iy, iz);
+        return cell_key(g, tab, ix, iy, iz, d);
     }
     return cell_key(g, tab, (int)p64.x[i], (int)p64.y[i], (int)p64.z[i], d);
 }
@@ -137,11 +181,12 @@ __device__ __forceinline__ void run_count(uint32_t *count, uint32_t key, bool ac
 // the first result is used (two in the FP64 scatter).  Launch bounds keep enough
 // warps resident: five CTAs of 256 per SM for the histogram, three for the FP32
 // scatter.
-template <bool F32>
+template <bool F32, bool LEAD = false>
 __global__ void __launch_bounds__(256, 5) k_hist(Geom g, const uint32_t *tab, PartF64 p64, PartF32 p32, int64_t seg, int64_t n,
-                       uint32_t *count, DevDiag *d)
+                       uint32_t *count, float h, DevDiag *d)
 {
-    constexpr int U = 4;
+    static_assert(F32 || !LEAD, "sort lead: FP32 form");
+    constexpr int U = LEAD ? 2 : 4;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += U * stride) {
         uint32_t key[U];
@@ -150,7 +195,7 @@ __global__ void __launch_bounds__(256, 5) k_hist(Geom g, const uint32_t *tab, Pa
         for (int u = 0; u < U; ++u) {
             const int64_t i = base + u * stride + threadIdx.x;
             act[u] = i < n;
-            key[u] = act[u] ? particle_key<F32>(g, tab, p64, p32, seg + i, d) : 0u;
+            key[u] = act[u] ? particle_key<F32>(g, tab, p64, p32, seg + i, LEAD ? h : 0.f, d) : 0u;
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) run_count(count, key[u], act[u]);
@@ -182,9 +227,15 @@ __device__ __forceinline__ void rec_load(const PartF64 &s64, const PartF32 &s32,
 }
 
 template <bool F32>
-__device__ __forceinline__ uint32_t rec_key(const Geom &g, const uint32_t *tab, const Rec<F32> &r, DevDiag *d)
+__device__ __forceinline__ uint32_t rec_key(const Geom &g, const uint32_t *tab, const Rec<F32> &r, float h,
+                                            DevDiag *d)
 {
-    if (F32) return cell_key(g, tab, cell_x(r.cell), cell_y(r.cell), cell_z(r.cell), d);
+    if (F32) {
+        if (h == 0.f) return cell_key(g, tab, cell_x(r.cell), cell_y(r.cell), cell_z(r.cell), d);
+        int ix, iy, iz;
+        lead_cell(g, r.cell, r.f, h, 10, d, ix, iy, iz);
+        return cell_key(g, tab, ix, iy, iz, d);
+    }
     return cell_key(g, tab, (int)r.a[0], (int)r.a[1], (int)r.a[2], d);
 }
 
@@ -202,7 +253,8 @@ __device__ __forceinline__ void rec32_store(int4 *rec, int64_t j, const Rec<true
 }
 
 __global__ void __launch_bounds__(256, 4) k_scatter_rec32(Geom g, const uint32_t *tab, PartF32 s32, const uint32_t *sid, int4 *rec,
-                                int64_t seg, int64_t n, const uint32_t *start, uint32_t *cursor, DevDiag *d)
+                                int64_t seg, int64_t n, const uint32_t *start, uint32_t *cursor, float h,
+                                DevDiag *d)
 {
     constexpr int U = 2;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -217,7 +269,7 @@ __global__ void __launch_bounds__(256, 4) k_scatter_rec32(Geom g, const uint32_t
             if (act[u]) rec_load<true>(PartF64{}, s32, sid, seg + i, r[u]);
         }
 #pragma unroll
-        for (int u = 0; u < U; ++u) key[u] = act[u] ? rec_key<true>(g, tab, r[u], d) : 0u;
+        for (int u = 0; u < U; ++u) key[u] = act[u] ? rec_key<true>(g, tab, r[u], h, d) : 0u;
         Agg agg[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) agg_issue(cursor, key[u], act[u], agg[u]);
@@ -269,7 +321,7 @@ __global__ void k_scatter_rec64(Geom g, const uint32_t *tab, PartF64 s64, const 
             if (act[u]) rec_load<false>(s64, PartF32{}, sid, seg + i, r[u]);
         }
 #pragma unroll
-        for (int u = 0; u < U; ++u) key[u] = act[u] ? rec_key<false>(g, tab, r[u], d) : 0u;
+        for (int u = 0; u < U; ++u) key[u] = act[u] ? rec_key<false>(g, tab, r[u], 0.f, d) : 0u;
 #pragma unroll
         for (int u = 0; u < U; ++u) slot[u] = aggregated_inc(cursor, key[u], act[u]);
 #pragma unroll
@@ -347,6 +399,15 @@ __device__ __forceinline__ uint32_t *stage_key_table(const Geom &g, const uint32
     return dst;
 }
 
+// The same key from the staged table, after the lead h (FP32 form).
+__device__ __forceinline__ uint32_t shared_key_lead(const Geom &g, const uint32_t *stab, int32_t c, const float f[6],
+                                                    float h, DevDiag *d)
+{
+    int ix, iy, iz;
+    lead_cell(g, c, f, h, 11, d, ix, iy, iz);
+    return stab[ix] + stab[g.nx + iy] + stab[g.nx + g.ny + iz];
+}
+
 __device__ __forceinline__ uint32_t shared_key(const Geom &g, const uint32_t *stab, int32_t c, DevDiag *d)
 {
     int ix = cell_x(c), iy = cell_y(c), iz = cell_z(c);
@@ -372,12 +433,16 @@ __device__ __forceinline__ uint32_t shared_key_xyz(const Geom &g, const uint32_t
 // Counts of source tile blockIdx.x: stay[] for the tile's own cells (plain
 // stores: every cell of every tile is written), imm[] (zeroed by the caller) by
 // global atomics.
-template <bool F32>
+// LEAD (FP32 form): keys after the sort lead h, from the offsets and velocities
+// as well as the cell.
+template <bool F32, bool LEAD = false>
 __global__ void __launch_bounds__(256) k_hist_tile(Geom g, const uint32_t *tab, PartF64 p64, PartF32 p32,
-                                                   const int64_t *tb, uint32_t *stay, uint32_t *imm, DevDiag *d)
+                                                   const int64_t *tb, uint32_t *stay, uint32_t *imm, float h,
+                                                   DevDiag *d)
 {
+    static_assert(F32 || !LEAD, "sort lead: FP32 form");
     extern __shared__ uint32_t sh[];
-    constexpr int U = F32 ? 8 : 4;
+    constexpr int U = F32 && !LEAD ? 8 : 4;
     const uint32_t C = (uint32_t)g.tile_cells, k0 = (uint32_t)blockIdx.x * C;
     for (uint32_t i = threadIdx.x; i < C; i += blockDim.x) sh[i] = 0u;
     const uint32_t *stab = stage_key_table(g, tab, sh + C);
@@ -386,7 +451,24 @@ __global__ void __launch_bounds__(256) k_hist_tile(Geom g, const uint32_t *tab, 
     for (int64_t base = lo; base < hi; base += U * (int64_t)blockDim.x) {
         uint32_t key[U];
         bool act[U];
-        if constexpr (F32) {
+        if constexpr (LEAD) {
+            int32_t cell[U];
+            float f[U][6];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {   // every load of the iteration first
+                const int64_t i = base + u * (int64_t)blockDim.x + threadIdx.x;
+                act[u] = i < hi;
+                cell[u] = act[u] ? p32.cell[i] : 0;
+                f[u][0] = act[u] ? p32.ox[i] : 0.f;
+                f[u][1] = act[u] ? p32.oy[i] : 0.f;
+                f[u][2] = act[u] ? p32.oz[i] : 0.f;
+                f[u][3] = act[u] ? p32.vx[i] : 0.f;
+                f[u][4] = act[u] ? p32.vy[i] : 0.f;
+                f[u][5] = act[u] ? p32.vz[i] : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) key[u] = act[u] ? shared_key_lead(g, stab, cell[u], f[u], h, d) : 0u;
+        } else if constexpr (F32) {
             int32_t cell[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {   // every load of the iteration first
@@ -425,7 +507,7 @@ template <bool F32>
 __global__ void __launch_bounds__(256, 4) k_scatter_tile(Geom g, const uint32_t *tab, PartF64 s64, PartF32 s32,
                                                          const uint32_t *sid, void *rec, const int64_t *tb,
                                                          int64_t seg, const uint32_t *start, const uint32_t *stay,
-                                                         uint32_t *imm, DevDiag *d)
+                                                         uint32_t *imm, float h, DevDiag *d)
 {
     extern __shared__ uint32_t sh[];
     constexpr int U = 2;
@@ -446,7 +528,10 @@ __global__ void __launch_bounds__(256, 4) k_scatter_tile(Geom g, const uint32_t 
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            if constexpr (F32) key[u] = act[u] ? shared_key(g, stab, r[u].cell, d) : 0u;
+            if constexpr (F32)
+                key[u] = act[u] ? (h != 0.f ? shared_key_lead(g, stab, r[u].cell, r[u].f, h, d)
+                                            : shared_key(g, stab, r[u].cell, d))
+                                : 0u;
             else key[u] = act[u] ? shared_key_xyz<F32>(g, stab, r[u].a[0], r[u].a[1], r[u].a[2], d) : 0u;
         }
         RunBump b[U];
@@ -579,7 +664,7 @@ __global__ void k_hist_multi(MultiSort m)
         for (int64_t base = first; base < last; base += blockDim.x) {
             const int64_t i = base + threadIdx.x;
             const bool active = i < last;
-            const uint32_t key = active ? particle_key<true>(sg.g, nullptr, PartF64{}, sg.p, sg.off + i, sg.diag) : 0u;
+            const uint32_t key = active ? particle_key<true>(sg.g, nullptr, PartF64{}, sg.p, sg.off + i, 0.f, sg.diag) : 0u;
             aggregated_inc(m.count + sg.key_base, key, active);
         }
     }
@@ -603,7 +688,7 @@ __global__ void k_scatter_multi(MultiSort m)
             const bool active = i < last;
             Rec<true> r;
             if (active) rec_load<true>(PartF64{}, sg.p, sg.ids, sg.off + i, r);
-            const uint32_t key = active ? rec_key<true>(sg.g, nullptr, r, sg.diag) : 0u;
+            const uint32_t key = active ? rec_key<true>(sg.g, nullptr, r, 0.f, sg.diag) : 0u;
             const uint32_t slot = aggregated_inc(m.cursor + sg.key_base, key, active);
             if (active) rec32_store(sg.rec, sg.off + (int64_t)(m.start[sg.key_base + key] - base0) + slot, r);
         }
@@ -718,7 +803,7 @@ constexpr size_t kTileSortMaxShared = 48 * 1024;
 // per species, tile-local counts, the scan of stayers + immigrants, tile starts,
 // then the tile-local scatter into records (FP32: left for the next push; FP64:
 // transposed back here).
-static void sort_tiles(ohpic_ctx *c)
+static void sort_tiles(ohpic_ctx *c, float h)
 {
     const Geom &g = c->g;
     const bool f32 = c->cfg.precision == OHPIC_FP32;
@@ -728,26 +813,31 @@ static void sort_tiles(ohpic_ctx *c)
         const int64_t n = c->count[s];
         int64_t *tb = c->tile_begin + (int64_t)s * (g.ntile + 1);
         cudaMemsetAsync(c->cell_count, 0, sizeof(uint32_t) * g.ncell, c->stream);
-        if (f32)
+        if (f32 && h != 0.f)
+            k_hist_tile<true, true><<<(unsigned)g.ntile, 256, smem, c->stream>>>(
+                g, c->key_table, c->p64[src], c->p32[src], tb, c->cell_stay, c->cell_count, h, c->diag);
+        else if (f32)
             k_hist_tile<true><<<(unsigned)g.ntile, 256, smem, c->stream>>>(g, c->key_table, c->p64[src], c->p32[src],
-                                                                          tb, c->cell_stay, c->cell_count, c->diag);
+                                                                          tb, c->cell_stay, c->cell_count, 0.f,
+                                                                          c->diag);
         else
             k_hist_tile<false><<<(unsigned)g.ntile, 256, smem, c->stream>>>(g, c->key_table, c->p64[src], c->p32[src],
-                                                                           tb, c->cell_stay, c->cell_count, c->diag);
+                                                                           tb, c->cell_stay, c->cell_count, 0.f,
+                                                                           c->diag);
         ++c->launches;
         scan_exclusive(c, c->cell_stay, c->cell_start, g.ncell, c->scan_tmp, c->cell_count);
         cudaMemsetAsync(c->cell_count, 0, sizeof(uint32_t) * g.ncell, c->stream);
         if (f32) {
             k_scatter_tile<true><<<(unsigned)g.ntile, 256, smem, c->stream>>>(
                 g, c->key_table, c->p64[src], c->p32[src], c->ids[src], c->pblock[dst], tb, c->seg[s], c->cell_start,
-                c->cell_stay, c->cell_count, c->diag);
+                c->cell_stay, c->cell_count, h, c->diag);
             ++c->launches;
             c->rec_pending = true;
         } else {
             double2 *rec = (double2 *)c->pblock[dst];
             k_scatter_tile<false><<<(unsigned)g.ntile, 256, smem, c->stream>>>(
                 g, c->key_table, c->p64[src], c->p32[src], c->ids[src], rec, tb, c->seg[s], c->cell_start,
-                c->cell_stay, c->cell_count, c->diag);
+                c->cell_stay, c->cell_count, 0.f, c->diag);
             k_rec64_to_soa<<<grid_of(n), 256, 0, c->stream>>>(rec, c->seg[s], n, c->p64[src], c->ids[src]);
             c->launches += 2;
         }
@@ -767,8 +857,12 @@ int sort_particles(ohpic_ctx *c)
     const int axes = g.nx + g.ny + g.nz;
     k_key_table<<<(unsigned)((axes + 255) / 256), 256, 0, c->stream>>>(g, c->key_table);
     ++c->launches;
+    // the lead in cells per unit velocity: sort_lead steps of the last step's dt
+    // (the configured dt before the first step)
+    const double dt = std::isfinite(c->sc_dt) ? c->sc_dt : c->cfg.dt;
+    const float h = f32 && c->sort_lead > 0 ? (float)(c->sort_lead * dt) : 0.f;
     if (c->sorted && sizeof(uint32_t) * ((size_t)g.tile_cells + axes) <= kTileSortMaxShared) {
-        sort_tiles(c);
+        sort_tiles(c, h);
         c->steps_since_sort = 0;
         return OHPIC_OK;
     }
@@ -778,11 +872,16 @@ int sort_particles(ohpic_ctx *c)
         cudaMemsetAsync(c->cell_count, 0, sizeof(uint32_t) * g.ncell, c->stream);
         if (n > 0) {
             if (f32)
-                k_hist<true><<<grid_of(n), 256, 0, c->stream>>>(g, c->key_table, c->p64[src], c->p32[src],
-                                                                c->seg[s], n, c->cell_count, c->diag);
+                if (h != 0.f)
+                    k_hist<true, true><<<grid_of(n), 256, 0, c->stream>>>(g, c->key_table, c->p64[src],
+                                                                          c->p32[src], c->seg[s], n, c->cell_count,
+                                                                          h, c->diag);
+                else
+                    k_hist<true><<<grid_of(n), 256, 0, c->stream>>>(g, c->key_table, c->p64[src], c->p32[src],
+                                                                    c->seg[s], n, c->cell_count, 0.f, c->diag);
             else
                 k_hist<false><<<grid_of(n), 256, 0, c->stream>>>(g, c->key_table, c->p64[src], c->p32[src],
-                                                                 c->seg[s], n, c->cell_count, c->diag);
+                                                                 c->seg[s], n, c->cell_count, 0.f, c->diag);
             ++c->launches;
         }
         scan_exclusive(c, c->cell_count, c->cell_start, g.ncell, c->scan_tmp);
@@ -796,7 +895,7 @@ int sort_particles(ohpic_ctx *c)
             if (f32) {
                 int4 *rec = (int4 *)c->pblock[dst];
                 k_scatter_rec32<<<grid_of(n), 256, 0, c->stream>>>(g, c->key_table, c->p32[src], c->ids[src], rec,
-                                                                   c->seg[s], n, c->cell_start, c->cell_count,
+                                                                   c->seg[s], n, c->cell_start, c->cell_count, h,
                                                                    c->diag);
                 ++c->launches;
                 c->rec_pending = true;

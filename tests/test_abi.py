@@ -167,3 +167,33 @@ def test_cpp_mirror_runs_the_path(ohpic, tmp_path):
     assert abs(float(words[6])) < 1e-9 * 256 * 100
     # the bounded solve: a positive potential at the charge, zero on the Dirichlet wall
     assert float(words[7]) > 0.0 and float(words[8]) == 0.0
+
+
+def test_struct_layouts_match_the_header(ohpic, tmp_path):
+    """The ctypes mirrors of the header's structs have the C compiler's sizes and
+    field offsets (a field added on one side only would shift the others)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc")
+    if not cc:
+        pytest.skip("no gcc")
+    pairs = [("ohpic_config", ohpic.Config), ("ohpic_diag", ohpic.Diag),
+             ("ohpic_species_init", ohpic.SpeciesInit), ("ohpic_tuning", ohpic.Tuning)]
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "ohpic.h"', 'int main(void) {']
+    for cname, py in pairs:
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ['return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60).stdout.split("\n")
+    got = {tuple(ln.split()[:2]): int(ln.split()[2]) for ln in out if ln.strip()}
+    for cname, py in pairs:
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)

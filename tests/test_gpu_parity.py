@@ -326,6 +326,56 @@ def test_sort_invariants(ohpic, oracle_mod):
         ctx.close()
 
 
+def test_sort_lead_files_particles_where_they_will_be(ohpic, oracle_mod):
+    """FP32 form with a sort lead of L steps: the first sort and a re-sort after
+    some steps file every particle under the cell it reaches moving straight on
+    for L steps (cell + floor(offset + v * L * dt) per axis, wrapped), in
+    tile-major order, with the same particles.  Particles whose advanced offset
+    lies within 1e-5 of a cell face are left out of the order check (the device
+    rounds the advanced offset to FP32 once)."""
+    P, O = ohpic, oracle_mod
+    setup = _two_species(O, (16, 16, 16), ppc=2)
+    lead = 5
+    o, ctx = _pair(P, O, setup, precision=1, tile=(8, 4, 8))
+    ctx.set_tuning(sort_lead=lead)
+    assert ctx.get_tuning()["sort_lead"] == lead
+    h = float(np.float32(lead * setup.dt))
+    moved = 0
+    for rnd in range(2):
+        if rnd:
+            ctx.step(setup.dt, 6)
+        before = [ctx.download(s) for s in range(2)]
+        ctx.sort()
+        for s in range(2):
+            dev = ctx.download(s, order=False)
+            ids = dev["ids"]
+            assert np.array_equal(np.sort(ids), np.arange(len(ids), dtype=np.uint32))
+            cells, far = [], np.ones(len(ids), dtype=bool)
+            for k, n in (("x", 16), ("y", 16), ("z", 16)):
+                c = np.floor(dev[k])
+                adv = (dev[k] - c) + dev["v" + k].astype(np.float32).astype(np.float64) * h
+                fl = np.floor(adv)
+                far &= np.abs(adv - np.round(adv)) > 1e-5
+                cells.append(((c + fl).astype(np.int64)) % n)
+                moved += int(np.count_nonzero(fl))
+            cx, cy, cz = cells
+            t = (cx // 8) + 2 * ((cy // 4) + 4 * (cz // 8))
+            key = t * 256 + (cx % 8) + 8 * ((cy % 4) + 4 * (cz % 8))
+            assert far.mean() > 0.99
+            assert np.all(np.diff(key[far]) >= 0)
+            back = ctx.download(s)
+            for k in KEYS:
+                np.testing.assert_array_equal(back[k], before[s][k])
+    assert moved > 100          # the lead changed the cell of many particles
+    ctx.close()
+    # the FP64 form sorts by the current cell only
+    o, ctx = _pair(P, O, setup, precision=0, tile=(8, 4, 8))
+    with pytest.raises(P.OhpicError):
+        ctx.set_tuning(sort_lead=lead)
+    assert ctx.get_tuning()["sort_lead"] == 0
+    ctx.close()
+
+
 def test_edge_positions_and_empty_species(ohpic, oracle_mod):
     """Particles on cell faces, at 0 and just below n, an empty species, and the
     rounding case where n + p rounds to n (wrapped to 0 by the second apply)."""

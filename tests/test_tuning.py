@@ -48,6 +48,7 @@ def test_fp32_state_identical_across_launch_shapes(ohpic):
     variants = [{"deposit": P.DEPOSIT_UNIFORM}, {"deposit": P.DEPOSIT_MATCH}, {"deposit": P.DEPOSIT_GROUPS},
                 {"deposit": P.DEPOSIT_RUNS}, {"lane_particles": 2, "deposit": P.DEPOSIT_LANES},
                 {"tile": (4, 4, 4)}, {"tile": (16, 8, 8)}, {"tile": (16, 8, 8), "deposit": P.DEPOSIT_GROUPS},
+                {"sort_lead": 5}, {"sort_lead": 5, "tile": (16, 8, 8)}, {"sort_lead": 3, "lane_particles": 2},
                 {"halo": 1},
                 {"halo": 3}, {"split": 3}, {"sort_every": 1}, {"sort_every": 100},
                 {"lane_particles": 2}, {"lane_particles": 2, "deposit": P.DEPOSIT_UNIFORM},
@@ -101,7 +102,8 @@ def test_autotuner_returns_a_valid_shape(ohpic):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("tuning", [{}, {"halo": 1, "split": 2}, {"deposit": "RUNS"}, {"tile": (16, 8, 8)}])
+@pytest.mark.parametrize("tuning", [{}, {"halo": 1, "split": 2}, {"deposit": "RUNS"}, {"tile": (16, 8, 8)},
+                                    {"tile": (16, 8, 8), "sort_lead": 4}])
 def test_push_from_sort_records_matches_arrays(ohpic, tuning):
     """The FP32 sort leaves its 32-byte records pending and the next push (four
     per lane, LANES deposit) reads them and writes the word arrays and ids
