@@ -53,7 +53,10 @@ typedef struct {
     int32_t tile_x;              /* largest tile edge along x (0 = 2 x tile, at most 64): a tile twice as
                                     long in x halves the halo share of the staged box and still
                                     leaves two CTAs per SM */
-    int32_t reserved[4];
+    int32_t sort_lead;           /* 0..4096: the cell sort files each particle under the cell it reaches
+                                    after this many steps of straight-line motion (0: its current cell;
+                                    the default config: half the default sort cadence) */
+    int32_t reserved[3];
 } ohpic_serve_config;
 
 typedef struct {

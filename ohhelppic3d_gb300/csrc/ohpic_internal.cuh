@@ -165,6 +165,7 @@ struct SortSeg {
     int64_t key_base;
     int64_t *tile_begin;     // ntile + 1 entries, absolute particle indices
     DevDiag *diag;
+    float h;                 // sort lead in cells per unit velocity (0: sort by the current cell)
 };
 constexpr int kMaxSortSegs = kMaxServeRuns * 2;
 constexpr int kSortChunk = 8192;   // particles per CTA pass

@@ -521,6 +521,7 @@ bool upload_tables(Server *s, std::vector<Run *> &runs)
             sg.key_base = P.key_base + ((int64_t)r->slot * P.f.nsp + k) * r->g.ncell;
             sg.tile_begin = r->tile_begin + (int64_t)k * (r->g.ntile + 1);
             sg.diag = r->diag;
+            sg.h = s->cfg.sort_lead > 0 ? (float)(s->cfg.sort_lead * r->sc[k].dt) : 0.f;
             chunks += (r->count[k] + kSortChunk - 1) / kSortChunk;
             hc[si] = (int32_t)chunks;
         }
@@ -1083,6 +1084,7 @@ void ohpic_serve_config_default(ohpic_serve_config *cfg)
     cfg->max_active = kMaxServeRuns;
     cfg->slots_per_pool = 16;
     cfg->sort_every = 8;
+    cfg->sort_lead = 4;
     cfg->use_graphs = 1;
     cfg->weights = OHPIC_WEIGHTS_REFERENCE;
     cfg->halo = 1;
@@ -1117,6 +1119,7 @@ static bool normalise(const ohpic_serve_config *in, ohpic_serve_config &c)
     if (c.slots_per_pool > 256) return false;
     if (c.sort_every < 0) return false;
     if (c.sort_every == 0) c.sort_every = 8;
+    if (c.sort_lead < 0 || c.sort_lead > 4096) return false;
     if (c.halo <= 0) c.halo = 1;
     if (c.halo > kMaxHalo) return false;
     if (c.tile < 0 || c.tile > 64 || c.tile_x < 0 || c.tile_x > 64) return false;

@@ -664,7 +664,7 @@ __global__ void k_hist_multi(MultiSort m)
         for (int64_t base = first; base < last; base += blockDim.x) {
             const int64_t i = base + threadIdx.x;
             const bool active = i < last;
-            const uint32_t key = active ? particle_key<true>(sg.g, nullptr, PartF64{}, sg.p, sg.off + i, 0.f, sg.diag) : 0u;
+            const uint32_t key = active ? particle_key<true>(sg.g, nullptr, PartF64{}, sg.p, sg.off + i, sg.h, sg.diag) : 0u;
             aggregated_inc(m.count + sg.key_base, key, active);
         }
     }
@@ -688,7 +688,7 @@ __global__ void k_scatter_multi(MultiSort m)
             const bool active = i < last;
             Rec<true> r;
             if (active) rec_load<true>(PartF64{}, sg.p, sg.ids, sg.off + i, r);
-            const uint32_t key = active ? rec_key<true>(sg.g, nullptr, r, 0.f, sg.diag) : 0u;
+            const uint32_t key = active ? rec_key<true>(sg.g, nullptr, r, sg.h, sg.diag) : 0u;
             const uint32_t slot = aggregated_inc(m.cursor + sg.key_base, key, active);
             if (active) rec32_store(sg.rec, sg.off + (int64_t)(m.start[sg.key_base + key] - base0) + slot, r);
         }

@@ -34,7 +34,7 @@ class ServeConfig(C.Structure):
                 ("slots_per_pool", C.c_int32), ("sort_every", C.c_int32), ("use_graphs", C.c_int32),
                 ("weights", C.c_int32), ("tile", C.c_int32), ("halo", C.c_int32), ("deposit", C.c_int32),
                 ("max_species", C.c_int32), ("lane_particles", C.c_int32), ("tile_x", C.c_int32),
-                ("reserved", C.c_int32 * 4)]
+                ("sort_lead", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class RunRequest(C.Structure):

@@ -177,9 +177,13 @@ def test_struct_layouts_match_the_header(ohpic, tmp_path):
     cc = shutil.which("gcc")
     if not cc:
         pytest.skip("no gcc")
+    from ohhelppic3d_gb300 import serve as S
     pairs = [("ohpic_config", ohpic.Config), ("ohpic_diag", ohpic.Diag),
-             ("ohpic_species_init", ohpic.SpeciesInit), ("ohpic_tuning", ohpic.Tuning)]
-    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "ohpic.h"', 'int main(void) {']
+             ("ohpic_species_init", ohpic.SpeciesInit), ("ohpic_tuning", ohpic.Tuning),
+             ("ohpic_serve_config", S.ServeConfig), ("ohpic_run_request", S.RunRequest),
+             ("ohpic_run_result", S.RunResult), ("ohpic_serve_stats", S.ServeStats)]
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "ohpic.h"', '#include "ohpic_serve.h"',
+             'int main(void) {']
     for cname, py in pairs:
         lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
         for fname, _ in py._fields_:

@@ -156,7 +156,8 @@ def test_run_identical_alone_and_in_the_mix(ohpic):
 def test_result_independent_of_sort_cadence_and_graphs(ohpic):
     probe = _probe((16, 16, 32), 17, (42, 78))
     ref, _ = _serve([probe], sort_every=10, use_graphs=1)
-    for kw in ({"sort_every": 1}, {"sort_every": 100}, {"use_graphs": 0}):
+    for kw in ({"sort_every": 1}, {"sort_every": 100}, {"use_graphs": 0}, {"sort_lead": 0},
+               {"sort_lead": 7, "sort_every": 3}):
         got, st = _serve([probe], **kw)
         _same_state(ref[0], got[0])
         if kw.get("use_graphs") == 0:
