@@ -49,6 +49,7 @@ def test_fp32_state_identical_across_launch_shapes(ohpic):
                 {"deposit": P.DEPOSIT_RUNS}, {"lane_particles": 2, "deposit": P.DEPOSIT_LANES},
                 {"tile": (4, 4, 4)}, {"tile": (16, 8, 8)}, {"tile": (16, 8, 8), "deposit": P.DEPOSIT_GROUPS},
                 {"sort_lead": 5}, {"sort_lead": 5, "tile": (16, 8, 8)}, {"sort_lead": 3, "lane_particles": 2},
+                {"tile": (16, 8, 8), "halo": 1}, {"tile": (16, 8, 8), "halo": 1, "sort_lead": 5},
                 {"halo": 1},
                 {"halo": 3}, {"split": 3}, {"sort_every": 1}, {"sort_every": 100},
                 {"lane_particles": 2}, {"lane_particles": 2, "deposit": P.DEPOSIT_UNIFORM},
