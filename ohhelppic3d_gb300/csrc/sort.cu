@@ -860,7 +860,8 @@ int sort_particles(ohpic_ctx *c)
     // the lead in cells per unit velocity: sort_lead steps of the last step's dt
     // (the configured dt before the first step)
     const double dt = std::isfinite(c->sc_dt) ? c->sc_dt : c->cfg.dt;
-    const float h = f32 && c->sort_lead > 0 ? (float)(c->sort_lead * dt) : 0.f;
+    float h = f32 && c->sort_lead > 0 ? (float)(c->sort_lead * dt) : 0.f;
+    if (!std::isfinite(h)) h = 0.f;   // no usable step yet: sort by the current cell
     if (c->sorted && sizeof(uint32_t) * ((size_t)g.tile_cells + axes) <= kTileSortMaxShared) {
         sort_tiles(c, h);
         c->steps_since_sort = 0;
