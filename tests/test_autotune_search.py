@@ -156,3 +156,34 @@ def test_near_ties_keep_the_current_choice_and_deposit_is_retuned_on_the_box(mon
     assert tuple(best0["tile"]) == (16, 8, 8) and best0["deposit"] == P.DEPOSIT_LANES
     first0 = [tr for tr in best0["trials"] if tuple(tr["tile"]) == (8, 8, 8) and tr["halo"] == 1]
     assert min(first0, key=lambda tr: tr["push_ms"])["deposit"] == P.DEPOSIT_RUNS
+
+
+def test_sort_lead_is_tuned_over_the_cycle(monkeypatch):
+    """A model in which a push costs by how far its particles are from where the
+    sort filed them: |steps since the sort - lead|.  Timed over a whole cycle
+    after the sort, half the cycle is the best lead; the FP64 form never tries
+    one (its sort files by the current cell only)."""
+    steps = 11                                     # a 12-step cycle: leads 0, 3 and 6
+
+    class LeadCtx(FakeCtx):
+        def __init__(self):
+            super().__init__()
+            self.t["sort_lead"] = 0
+
+        def step(self, dt, n=1):
+            for _ in range(n):
+                if self.timing:
+                    self.push_ms += cost(self.t, 0) + 0.4 * abs(self.since - self.t["sort_lead"])
+                    self.push_launches += 1
+                self.since += 1
+
+    monkeypatch.setattr(A, "_ctx", lambda cfg_kw, species, seed=(42, 4242): LeadCtx())
+    monkeypatch.setattr(A, "_sort_ms", lambda ctx: (ctx.sort(), 1.0)[1])
+    best = A.tune(n=(64, 32, 32), dt=0.1, b0=(0, 0, 0.5), qm=[-1.0], q=[1.0], capacity_per_cell=[9.0],
+                  species=[None], steps=steps, max_cadence=5)
+    assert best["sort_lead"] == 6
+    assert sorted({tr["sort_lead"] for tr in best["trials"]}) == [0, 3, 6]
+    best64 = A.tune(n=(64, 32, 32), dt=0.1, b0=(0, 0, 0.5), qm=[-1.0], q=[1.0], capacity_per_cell=[9.0],
+                    species=[None], steps=steps, max_cadence=5, precision=P.FP64)
+    assert best64["sort_lead"] == 0
+    assert all(tr["sort_lead"] == 0 for tr in best64["trials"])
