@@ -499,7 +499,7 @@ def accuracy_block(caps32: dict, caps64: dict, weights: int) -> dict:
 # ---------------------------------------------------------------------------
 # Serving: the ensemble of small runs through the continuous-batching server
 # ---------------------------------------------------------------------------
-def sequential_runs(P, reqs, sort_every: int, sort_lead: int, weights: int) -> dict:
+def sequential_runs(P, reqs, sort_every: int, sort_lead: int, weights: int, halo: int = 1) -> dict:
     """One run at a time on the single-context API: create, draw, step, read the
     diagnostics, destroy.  Times with and without the per-run set-up.  The runs
     get the server's launch shape, cadence and sort lead."""
@@ -513,10 +513,10 @@ def sequential_runs(P, reqs, sort_every: int, sort_lead: int, weights: int) -> d
         cfg = P.make_config(n=r.n, dt=r.dt, b0=r.b0, qm=r.qm, q=r.q, capacity=caps, precision=P.FP32,
                             weights=weights, sort_every=sort_every)
         with P.PicContext(cfg) as ctx:
-            # the server's launch shape: halo 1, tile edges up to 16 in x and 8 in y, z
+            # the server's launch shape: its halo, tile edges up to 16 in x and 8 in y, z
             tile = tuple(max(t for t in (1, 2, 4, 8, 16) if t <= want and n % t == 0)
                          for n, want in zip(r.n, (16, 8, 8)))
-            ctx.set_tuning(halo=1, tile=tile, sort_lead=sort_lead)
+            ctx.set_tuning(halo=halo, tile=tile, sort_lead=sort_lead)
             counts = ctx.init_particles(r.species, seed=r.seed)
             ctx.synchronize()
             t1 = time.perf_counter()
@@ -550,24 +550,26 @@ def run_serving(P, args) -> dict:
     n_runs, scale = args.serve_runs, args.serve_step_scale
     sat_reqs = S.ensemble_stream(n_runs, rate=None, step_scale=scale)
     lead = args.serve_sort_every // 2 if args.serve_sort_lead < 0 else args.serve_sort_lead
-    with S.Server(sort_every=args.serve_sort_every, sort_lead=lead, weights=args.weights) as srv:
+    with S.Server(sort_every=args.serve_sort_every, sort_lead=lead, halo=args.serve_halo,
+                  weights=args.weights) as srv:
         sat = S.run_stream(srv, sat_reqs)
         sat_stats = srv.stats()
     mean_work = sat["particle_steps"] / n_runs
     rate = 0.8 * sat["throughput"] / mean_work
     reqs = S.ensemble_stream(n_runs, rate=rate, step_scale=scale)
-    with S.Server(sort_every=args.serve_sort_every, sort_lead=lead, weights=args.weights) as srv:
+    with S.Server(sort_every=args.serve_sort_every, sort_lead=lead, halo=args.serve_halo,
+                  weights=args.weights) as srv:
         poi = S.run_stream(srv, reqs)
         poi_stats = srv.stats()
     k = min(args.serve_sequential, n_runs)
-    seq = sequential_runs(P, sat_reqs[:k], args.serve_sort_every, lead, args.weights)
+    seq = sequential_runs(P, sat_reqs[:k], args.serve_sort_every, lead, args.weights, args.serve_halo)
     keep = ("ticks", "sort_ticks", "graph_captures", "graph_launches", "launches", "bytes_peak", "pools")
     return {
         "workload": (f"{n_runs} periodic FP32 runs: grids {{16,24,32,48,64}}^3, ppc per species {{8,16,32,64}}, "
                      f"wce/wpe~U[0,1], vth_e~U[0.5,2], vth_i=vth_e/10, mass ratio 100, dt=0.1, "
                      f"steps~U{{200..2000}} x {scale}; parameter stream pcg32 (42, 1000), run i seeded (42, 52+i)"),
         "runs": n_runs, "step_scale": scale, "weights": _wname(args.weights), "particle_steps": sat["particle_steps"],
-        "sort_every": args.serve_sort_every, "sort_lead": lead,
+        "sort_every": args.serve_sort_every, "sort_lead": lead, "halo": args.serve_halo,
         "saturated": {"throughput": sat["throughput"], "span_s": sat["span_s"], "p50_s": sat["p50_s"],
                       "p99_s": sat["p99_s"], "stats": {k2: sat_stats[k2] for k2 in keep}},
         "poisson_80": {"rate_runs_per_s": rate, "throughput": poi["throughput"], "span_s": poi["span_s"],
@@ -687,6 +689,7 @@ def main(argv=None) -> int:
     ap.add_argument("--serve-runs", type=int, default=512)
     ap.add_argument("--serve-step-scale", type=float, default=1.0)
     ap.add_argument("--serve-sort-every", type=int, default=8)
+    ap.add_argument("--serve-halo", type=int, default=1, help="staged halo of the served and one-at-a-time runs")
     ap.add_argument("--serve-sort-lead", type=int, default=-1,
                     help="sort lead of the served and one-at-a-time runs (-1: half the cadence)")
     ap.add_argument("--serve-sequential", type=int, default=32, help="runs timed one at a time")
