@@ -180,11 +180,13 @@ int ohpic_push(ohpic_ctx *ctx, double dt);
  * Scatters first if rho is stale. */
 int ohpic_step(ohpic_ctx *ctx, double dt, int nsteps);
 
-/* Periodic counting sort of every species by tile-major cell index.  In the
- * FP32 form the sort leaves each particle as a 32-byte record; the next
- * ohpic_push/ohpic_step in the default launch shape reads the records and
- * writes the particle arrays itself, and every other call that touches
- * particles converts them first.  Callers see no difference but the timing. */
+/* Periodic counting sort of every species by tile-major cell index (in the
+ * FP32 form with ohpic_tuning.sort_lead > 0: the cell each particle reaches
+ * after that many steps of straight-line motion).  In the FP32 form the sort
+ * leaves each particle as a 32-byte record; the next ohpic_push/ohpic_step in
+ * the default launch shape reads the records and writes the particle arrays
+ * itself, and every other call that touches particles converts them first.
+ * Callers see no difference but the timing and the storage order. */
 int ohpic_sort(ohpic_ctx *ctx);
 
 /* Field exchange, nx*ny*nz doubles with x fastest.  Uploading rho or E
