@@ -59,3 +59,29 @@ def test_reference_arm_line(monkeypatch):
     assert line["config"]["weights"] == "standard CIC"
     # measured directly: ms_per_step x steps is the measured time of 1,048,576 particles
     assert abs(line["value"] * line["ms_per_step"] / 1e3 - 1048576) < 1e-6 * 1048576
+
+
+def test_tuning_block_keeps_the_sort_lead(monkeypatch):
+    """The bench carries the autotuner's sort lead into the applied tuning, and
+    counts the record pushes of a run the same way with or without a lead."""
+    from types import SimpleNamespace
+
+    import ohhelppic3d_gb300 as P
+    from ohhelppic3d_gb300 import autotune
+
+    seen = {}
+
+    def fake_tune(**kw):
+        seen.update(kw)
+        return {"tile": (16, 8, 8), "halo": 2, "split": 1, "deposit": P.DEPOSIT_LANES, "lane_particles": 4,
+                "sort_lead": 10, "sort_every": 19, "grid_tuned_on": (256, 128, 64), "trials": [{}] * 3}
+
+    monkeypatch.setattr(autotune, "tune", fake_tune)
+    args = SimpleNamespace(tuning=None, no_tune=False)
+    t = bench.tune_form(P, c2(), "fp32", args, 1)
+    assert t["sort_lead"] == 10 and t["tile"] == (16, 8, 8) and t["trials"] == 3
+    assert seen["steps"] == c2().sort_every - 1 and seen["precision"] == P.FP32
+    applied = {"lane_particles": 4, "deposit": P.DEPOSIT_LANES, "sort_lead": 10}
+    assert bench.record_pushes("fp32", applied, 20, 20, P.DEPOSIT_LANES) == 1
+    assert bench.record_pushes("fp32", dict(applied, sort_lead=0), 40, 20, P.DEPOSIT_LANES) == 2
+    assert bench.record_pushes("fp64", applied, 20, 20, P.DEPOSIT_LANES) == 0
